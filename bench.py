@@ -1,0 +1,367 @@
+"""Benchmark: progressive insertion throughput (points inserted/s) at
+recall@15 >= 0.95 on the 70,000 x 784 image-like workload, k=15, euclidean,
+500 points per cycle.
+
+One step = one complete progressive build: 140 cycles of
+run_with_n_ops(500, U, E) followed by F full update cycles, then a recall@15
+check on 2,000 seeded query rows against an exact FP64 brute force.
+
+* ``value``  -- the C ABI with the input already resident in HBM
+  (gm_append_device), CUDA-event timed on the device.
+* ``e2e``    -- the public Python API (gpumap_gb300.GPUMAP over pinned host
+  chunks; every cycle copies its 500 rows host->device, each step ends by
+  reading the k-NN table back to the host).
+* ``roofline`` -- the local-join kernel's algorithmic bytes over its own
+  CUDA-event time (events recorded by the engine on its stream).
+* ``cpu_baseline`` / ``--impl reference`` -- the CPU restatement of the
+  reference path (oracle/) on a bounded sample of the same workload.
+
+Multi-GPU (torchrun): replicas only -- every rank builds its own copy of the
+workload on its own GPU; no collective is on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_POINTS, N_FEATURES, K = 70_000, 784, 15
+CHUNK = 500
+UPD_OPS, EMB_OPS = 2000, 1000
+FINAL_UPDATE_CYCLES = 3
+MAX_EPOCH = 200
+RECALL_QUERIES = 2000
+METRIC = "points inserted/s at recall@15>=0.95 (70k x 784, k=15, 500 points/cycle)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--update-ops", type=int, default=UPD_OPS)
+    ap.add_argument("--embedding-ops", type=int, default=EMB_OPS)
+    ap.add_argument("--final-updates", type=int, default=FINAL_UPDATE_CYCLES)
+    ap.add_argument("--n-points", type=int, default=N_POINTS)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
+                                           "--format=csv,noheader,nounits", "-lms", "200"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def exact_knn_gpu(X_dev, q_idx, k):
+    """Exact neighbours of the query rows in float64 on the GPU (recall check)."""
+    import torch
+
+    Xd = X_dev.double()
+    sq = (Xd * Xd).sum(1)
+    out = []
+    for s in range(0, len(q_idx), 256):
+        qq = torch.as_tensor(q_idx[s : s + 256], device=Xd.device)
+        d = sq[qq, None] + sq[None, :] - 2.0 * (Xd[qq] @ Xd.T)
+        d[torch.arange(len(qq), device=d.device), qq] = float("inf")
+        out.append(torch.topk(d, k, largest=False).indices.cpu().numpy())
+    return np.concatenate(out)
+
+
+def recall(approx, exact):
+    k = exact.shape[1]
+    return float(np.mean([len(set(a.tolist()) & set(e.tolist())) / k for a, e in zip(approx, exact)]))
+
+
+def flush_l2(buf):
+    buf.zero_()
+
+
+def run_value_step(native, X_dev, n, d, upd, emb, final, stats_on):
+    import torch
+
+    p = native.default_params(n_instances=n, n_features=d, n_neighbors=K, max_epoch=MAX_EPOCH,
+                              device=torch.cuda.current_device())
+    p.a, p.b = 1.5769434602697652, 0.8950608778515733  # find_ab_params(1.0, 0.1)
+    s = native.Session(p)
+    s.set_stats(stats_on)
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record()
+    base = X_dev.data_ptr()
+    row_bytes = d * 4
+    for c in range(0, n, CHUNK):
+        m = min(CHUNK, n - c)
+        s.append_device(base + c * row_bytes, m, d)
+        s.run(m, upd, emb)
+    for _ in range(final):
+        s.run(0, n, 0)
+    end.record()
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end)
+    st = s.stats()
+    v = s.view("indices")
+    idx = torch.as_tensor(_Cai(v.ptr, n, K + 1, 4, "<u4"), device="cuda")[:, :K]
+    return s, ms, st, idx
+
+
+class _Cai:
+    def __init__(self, ptr, rows, cols, esz, typestr):
+        self.__cuda_array_interface__ = {"version": 3, "shape": (rows, cols), "typestr": typestr,
+                                         "strides": (cols * esz, esz), "data": (ptr, True)}
+
+
+def run_e2e_step(X_host, n, d, upd, emb, final):
+    import torch
+
+    import gpumap_gb300 as gm
+    from gpumap_gb300.data_loader import ArrayDataLoader
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    params = gm.GPUMAPParams()
+    params.n_instances, params.n_features, params.n_neighbors = n, d, K
+    params.max_epoch = MAX_EPOCH
+    model = gm.GPUMAP(ArrayDataLoader(X_host), params)
+    for c in range(0, n, CHUNK):
+        model.run_with_n_ops(min(CHUNK, n - c), upd, emb)
+    for _ in range(final):
+        model.run_with_n_ops(0, n, 0)
+    idx = model.get_neighbor_indices().cpu().numpy()  # the step's result, device -> host
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    model.close()
+    return dt, idx
+
+
+def cpu_baseline_sample(X, upd, emb, cycles=2):
+    """Oracle (CPU restatement of the reference path) on the first cycles of
+    the workload: points inserted per second, single thread."""
+    from oracle.session import OracleSession
+
+    n = cycles * CHUNK
+    o = OracleSession(n, X.shape[1], k=K, max_epoch=MAX_EPOCH, a=1.5769434602697652, b=0.8950608778515733)
+    t0 = time.perf_counter()
+    for c in range(cycles):
+        o.append(X[c * CHUNK : (c + 1) * CHUNK])
+        o.run(CHUNK, min(upd, n), min(emb, n))
+    dt = time.perf_counter() - t0
+    return n / dt, dt, n
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    from gpumap_gb300.datasets import image_like
+
+    n, d = args.n_points, N_FEATURES
+    X, _ = image_like(n, d, seed=0)
+    config = {"workload": f"image-like mixture {n}x{d}, k={K}, euclidean, {CHUNK} points/cycle, "
+                          f"run_with_n_ops({CHUNK},{args.update_ops},{args.embedding_ops}) then "
+                          f"{args.final_updates} x run_with_n_ops(0,{n},0)",
+              "n_points": n, "n_features": d, "n_neighbors": K, "max_epoch": MAX_EPOCH,
+              "update_ops": args.update_ops, "embedding_ops": args.embedding_ops,
+              "final_update_cycles": args.final_updates, "l2": "inputs (220 MB) larger than L2; 512 MB flush between steps",
+              "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        steps = []
+        for i in range(args.warmup + args.steps):
+            v, dt, npts = cpu_baseline_sample(X, args.update_ops, args.embedding_ops, cycles=1)
+            if i >= args.warmup:
+                steps.append((v, dt))
+        val = statistics.median([v for v, _ in steps])
+        line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "points/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * statistics.median([t for _, t in steps]),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": config,
+                "cpu_baseline": {"value": val, "unit": "points/s", "cores": 1, "kind": "port",
+                                 "sample": f"first {CHUNK} rows, one cycle run_with_n_ops({CHUNK},{args.update_ops},{args.embedding_ops}); "
+                                           "the reference's CUDA build is unavailable (needs RAFT/RMM, CUDA 12.6)"},
+                "e2e": {"value": val, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from gpumap_gb300 import _native
+
+    native = _native
+    native.load()
+    X_dev = torch.from_numpy(X).cuda()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    q_idx = np.random.default_rng(123).choice(n, min(RECALL_QUERIES, n), replace=False)
+    exact = exact_knn_gpu(X_dev, q_idx, K)
+
+    for _ in range(args.warmup):
+        s, _, _, _ = run_value_step(native, X_dev, n, d, args.update_ops, args.embedding_ops, args.final_updates, False)
+        del s
+    barrier(world)
+    times, recalls, launches, join = [], [], 0, []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            barrier(world)
+            s, ms, st, idx = run_value_step(native, X_dev, n, d, args.update_ops, args.embedding_ops,
+                                            args.final_updates, True)
+            times.append(ms)
+            launches += st.kernel_launches
+            join.append((st.join_ms, st.join_rows, st.join_pairs, st.join_launches, st.cand_ms, st.cand_rows,
+                         st.cand_launches, st.sgd_ms, list(st.phase_s)))
+            recalls.append(recall(idx.to(torch.int64).cpu().numpy()[q_idx], exact))
+            del s
+    total_ms = max_over_ranks(sum(times), world)
+    ms_step = total_ms / args.steps
+    value = world * n * args.steps / (total_ms / 1000.0)
+
+    # roofline: local join (dominant update kernel) and candidate distances
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    j_ms = sum(j[0] for j in join)
+    j_bytes = sum(j[1] * d * 4 + j[2] * 8 for j in join)
+    c_ms = sum(j[4] for j in join)
+    c_bytes = sum(j[5] * d * 4 for j in join)
+    j_launch = sum(j[3] for j in join)
+    c_launch = sum(j[6] for j in join)
+    dominant = "local_join" if j_ms >= c_ms else "candidate_dists"
+    if dominant == "local_join":
+        ach = (j_bytes / max(j_launch, 1)) / ((j_ms / max(j_launch, 1)) / 1000.0) / 1e9 if j_ms > 0 else 0.0
+    else:
+        ach = (c_bytes / max(c_launch, 1)) / ((c_ms / max(c_launch, 1)) / 1000.0) / 1e9 if c_ms > 0 else 0.0
+    traffic_path = ROOT / "profiles" / "traffic.json"
+    traffic = None
+    if traffic_path.exists():
+        traffic = json.loads(traffic_path.read_text()).get(dominant)
+    line = {
+        "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded image-like mixture, 70k x 784)",
+        "config": config,
+        "recall_at_15": min(recalls), "recall_valid": min(recalls) >= 0.95,
+        "gpu_launches": int(launches),
+        "roofline": {"kernel": dominant, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                     "frac": ach / hbm if hbm else None, "traffic": traffic, "peak_source": "measured"},
+        "kernel_time_ms": {"local_join": j_ms / args.steps, "candidate_dists": c_ms / args.steps,
+                           "sgd": sum(j[7] for j in join) / args.steps},
+        "phase_s": [sum(j[8][i] for j in join) / args.steps for i in range(3)],
+    }
+    line["clocks"] = clk.summary()
+
+    if not args.no_e2e:
+        X_pin = torch.from_numpy(X).pin_memory().numpy()
+        run_e2e_step(X_pin, n, d, args.update_ops, args.embedding_ops, args.final_updates)  # warm
+        e2e_t, e2e_rec = [], []
+        for _ in range(max(1, min(args.steps, 3))):
+            flush_l2(flush)
+            dt, idx = run_e2e_step(X_pin, n, d, args.update_ops, args.embedding_ops, args.final_updates)
+            e2e_t.append(dt)
+            e2e_rec.append(recall(idx.astype(np.int64)[q_idx], exact))
+        tmax = max_over_ranks(sum(e2e_t), world)
+        line["e2e"] = {"value": world * n * len(e2e_t) / tmax, "unit": "points/s",
+                       "h2d_bytes_per_step": n * d * 4, "d2h_bytes_per_step": n * K * 4,
+                       "recall_at_15": min(e2e_rec)}
+    if rank == 0 and not args.no_cpu_baseline:
+        v, dt, npts = cpu_baseline_sample(X, args.update_ops, args.embedding_ops, cycles=2)
+        line["cpu_baseline"] = {"value": v, "unit": "points/s", "cores": 1, "kind": "port",
+                                "sample": f"first {npts} rows in {npts // CHUNK} cycles of run_with_n_ops({CHUNK},"
+                                          f"{args.update_ops},{args.embedding_ops}), {dt:.1f} s, CPU restatement"}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

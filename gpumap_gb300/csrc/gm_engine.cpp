@@ -1,0 +1,619 @@
+// Session engine: host-side policy of the progressive cycle, all numeric
+// state on the device.  The queue, cursor, seed and completion rules restate
+// the reference's GPUMAP::Impl (impl.cuh:29-533); the O(n) host copies and
+// host merges of the reference are replaced by device kernels, so per-cycle
+// host work and PCIe/C2C traffic scale with the batch, not with n.
+#include "gm_engine.h"
+
+#include "gm_common.cuh"
+
+#include <algorithm>
+#include <cfloat>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <unordered_set>
+
+namespace gm {
+
+namespace {
+
+using Clock = std::chrono::high_resolution_clock;
+
+void ck(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return;
+  cudaGetLastError();
+  if (e == cudaErrorMemoryAllocation)
+    throw Error(GM_ERR_OOM, std::string(what) + ": " + cudaGetErrorString(e));
+  throw Error(GM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+size_t round_up(size_t v, size_t m) { return (v + m - 1) / m * m; }
+
+}  // namespace
+
+template <typename... A>
+void Session::log(const char *fmt, A... a) const {
+  if (p_.verbose) {
+    std::fprintf(stderr, fmt, a...);
+    std::fflush(stderr);
+  }
+}
+
+Session::Session(const gm_params &p) : p_(p) {
+  if (p.n_components != 2)
+    throw Error(GM_ERR_INVALID, "n_components must be 2");
+  if (p.n_neighbors < 1 || p.n_neighbors > (uint64_t)kListW)
+    throw Error(GM_ERR_INVALID, "n_neighbors must be in [1, 32]");
+  if (p.n_features < 1) throw Error(GM_ERR_INVALID, "n_features must be >= 1");
+  if (p.metric != GM_METRIC_EUCLIDEAN && p.metric != GM_METRIC_COSINE)
+    throw Error(GM_ERR_INVALID, "unknown metric");
+  if (p.precision != 0) throw Error(GM_ERR_INVALID, "precision must be 0 (FP32)");
+  if (p.n_instances > (uint64_t)(1u << 30))
+    throw Error(GM_ERR_INVALID, "n_instances exceeds 2^30");
+  if (p.n_features > (uint64_t)(1u << 24)) throw Error(GM_ERR_INVALID, "n_features too large");
+
+  if (p.device >= 0) ck(cudaSetDevice(p.device), "cudaSetDevice");
+  ck(cudaGetDevice(&device_), "cudaGetDevice");
+  ck(cudaFree(nullptr), "CUDA context");
+  ck(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+
+  const size_t N = p.n_instances, d = p.n_features, k = p.n_neighbors;
+  st_.n_cap = (int)N;
+  st_.d = (int)d;
+  st_.ld = (int)round_up(d, 4);
+  st_.k = (int)k;
+  st_.cosine = p.metric == GM_METRIC_COSINE;
+  const size_t Nm = std::max<size_t>(N, 1);
+
+  auto dalloc = [&](size_t bytes) -> void * {
+    void *ptr = nullptr;
+    ck(cudaMalloc(&ptr, std::max<size_t>(bytes, 16)), "cudaMalloc");
+    allocs_.push_back(ptr);
+    return ptr;
+  };
+  try {
+    st_.X = (float *)dalloc(Nm * st_.ld * sizeof(float));
+    st_.norms = (float *)dalloc(Nm * sizeof(float));
+    st_.g_ids = (int *)dalloc(Nm * kListW * sizeof(int));
+    st_.g_dists = (float *)dalloc(Nm * kListW * sizeof(float));
+    st_.locks = (int *)dalloc(Nm * sizeof(int));
+    st_.dirty = (int *)dalloc(Nm * sizeof(int));
+    st_.knn_ids = (int *)dalloc(Nm * k * sizeof(int));
+    st_.knn_dists = (float *)dalloc(Nm * k * sizeof(float));
+    st_.pub_idx = (uint32_t *)dalloc(Nm * (k + 1) * sizeof(uint32_t));
+    st_.pub_dist = (float *)dalloc(Nm * (k + 1) * sizeof(float));
+    st_.emb = (float *)dalloc(Nm * 2 * sizeof(float));
+    st_.bloom = (uint32_t *)dalloc(Nm * 64 * sizeof(uint32_t));
+    st_.err = (unsigned *)dalloc(16);
+    d_stat_ = (unsigned long long *)dalloc(8 * sizeof(unsigned long long));
+    st_.stat = d_stat_;
+
+    us_.fwd_new = (int *)dalloc(Nm * kSamples * sizeof(int));
+    us_.fwd_old = (int *)dalloc(Nm * kSamples * sizeof(int));
+    us_.rev_new = (int *)dalloc(Nm * kSamples * sizeof(int));
+    us_.rev_old = (int *)dalloc(Nm * kSamples * sizeof(int));
+    us_.sizes = (int4 *)dalloc(Nm * sizeof(int4));
+    us_.cnt = (int *)dalloc(Nm * sizeof(int));
+    us_.off = (int *)dalloc((Nm + 1) * sizeof(int));
+    us_.fill = (int *)dalloc(Nm * sizeof(int));
+    us_.csr = (int *)dalloc(Nm * kSamples * sizeof(int));
+    us_.hflag = (int *)dalloc(Nm * sizeof(int));
+
+    d_rows_ = (int *)dalloc(Nm * sizeof(int));
+    d_rows2_ = (int *)dalloc(Nm * sizeof(int));
+    d_batch_ = (int *)dalloc(Nm * sizeof(int));
+    d_cnt_ = (int *)dalloc(16 * sizeof(int));
+    d_tmp_ = (int *)dalloc(std::max(scan_tmp_ints((int)Nm), compact_tmp_ints((int)Nm)) *
+                           sizeof(int) + 64);
+
+    es_.flag = (int *)dalloc(Nm * sizeof(int));
+    es_.unsel = (int *)dalloc(Nm * sizeof(int));
+    es_.sigma = (float *)dalloc(Nm * sizeof(float));
+    es_.rho = (float *)dalloc(Nm * sizeof(float));
+    es_.deg = (int *)dalloc(Nm * sizeof(int));
+    es_.snap = (float *)dalloc(Nm * 2 * sizeof(float));
+    es_.fscal = (float *)dalloc(16 * sizeof(float));
+    es_.iscal = (int *)dalloc(16 * sizeof(int));
+    es_.cap_partial = (Nm * k + 255) / 256 + 512;
+    es_.partial = (float *)dalloc(es_.cap_partial * 2 * sizeof(float));
+    es_.ipartial = (int *)dalloc(es_.cap_partial * sizeof(int));
+    es_.batch = d_batch_;
+    es_.tmp = d_tmp_;
+
+    ck(cudaMallocHost((void **)&h_pin_, (Nm + 64) * sizeof(uint32_t)), "cudaMallocHost");
+  } catch (...) {
+    for (void *q : allocs_) cudaFree(q);
+    allocs_.clear();
+    if (h_pin_) cudaFreeHost(h_pin_);
+    if (stream_) cudaStreamDestroy(stream_);
+    throw;
+  }
+
+  // Initial contents: zero features (padding must stay zero), empty lists,
+  // "no neighbour" published rows, zero embedding.
+  cudaStream_t s = stream_;
+  const uint32_t kFltMaxBits = 0x7f7fffffu;  // FLT_MAX
+  ck(cudaMemsetAsync(st_.X, 0, Nm * st_.ld * sizeof(float), s), "memset");
+  ck(cudaMemsetAsync(st_.norms, 0, Nm * sizeof(float), s), "memset");
+  fill_u32(st_.g_ids, (uint32_t)kIdSentinel, Nm * kListW, s);
+  fill_u32(st_.g_dists, kFltMaxBits, Nm * kListW, s);
+  ck(cudaMemsetAsync(st_.locks, 0, Nm * sizeof(int), s), "memset");
+  ck(cudaMemsetAsync(st_.dirty, 0, Nm * sizeof(int), s), "memset");
+  fill_u32(st_.knn_ids, (uint32_t)kIdSentinel, Nm * k, s);
+  fill_u32(st_.knn_dists, kFltMaxBits, Nm * k, s);
+  fill_u32(st_.pub_idx, kPubIdxSentinel, Nm * (k + 1), s);
+  fill_u32(st_.pub_dist, kFltMaxBits, Nm * (k + 1), s);
+  ck(cudaMemsetAsync(st_.emb, 0, Nm * 2 * sizeof(float), s), "memset");
+  ck(cudaMemsetAsync(st_.bloom, 0, Nm * 64 * sizeof(uint32_t), s), "memset");
+  ck(cudaMemsetAsync(st_.err, 0, 16, s), "memset");
+  ck(cudaMemsetAsync(d_stat_, 0, 8 * sizeof(unsigned long long), s), "memset");
+  ck(cudaMemsetAsync(us_.sizes, 0, Nm * sizeof(int4), s), "memset");
+  ck(cudaMemsetAsync(es_.sigma, 0, Nm * sizeof(float), s), "memset");
+  ck(cudaMemsetAsync(es_.rho, 0, Nm * sizeof(float), s), "memset");
+  ck(cudaMemsetAsync(es_.iscal, 0, 16 * sizeof(int), s), "memset");
+  ck(cudaMemsetAsync(es_.fscal, 0, 16 * sizeof(float), s), "memset");
+  ck(cudaGetLastError(), "init fill");
+  ck(cudaStreamSynchronize(s), "init sync");
+  upd_q_.reset(N);
+  ensure_embed(1);
+}
+
+Session::~Session() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  for (auto &e : ev_pool_) cudaEventDestroy(e);
+  for (auto &pr : ev_pending_) {
+    cudaEventDestroy(pr.a);
+    cudaEventDestroy(pr.b);
+  }
+  for (void *q : allocs_) cudaFree(q);
+  if (cand_) cudaFree(cand_);
+  if (cand_cnt_) cudaFree(cand_cnt_);
+  if (cand_dist_) cudaFree(cand_dist_);
+  if (es_.coo_row) {
+    cudaFree(es_.coo_row);
+    cudaFree(es_.coo_col);
+    cudaFree(es_.coo_val);
+    cudaFree(es_.t_row);
+    cudaFree(es_.t_col);
+    cudaFree(es_.flag_tail);
+    cudaFree(es_.t_val);
+    cudaFree(es_.next_s);
+    cudaFree(es_.next_n);
+    cudaFree(es_.tmp2);
+  }
+  if (h_pin_) cudaFreeHost(h_pin_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+void Session::sync() { ck(cudaStreamSynchronize(stream_), "cudaStreamSynchronize"); }
+
+void Session::check_device_error(const char *phase) {
+  unsigned e = 0;
+  ck(cudaMemcpyAsync(&e, st_.err, sizeof(unsigned), cudaMemcpyDeviceToHost, stream_), "err");
+  sync();
+  if (e != 0u) {
+    cudaMemsetAsync(st_.err, 0, sizeof(unsigned), stream_);
+    throw Error(GM_ERR_DEVICE, std::string(phase) + ": a bounded device wait ran out (bits " +
+                                   std::to_string(e) + ")");
+  }
+}
+
+void Session::ensure_cand(size_t rows) {
+  if (rows <= cand_rows_) return;
+  sync();
+  if (cand_) cudaFree(cand_);
+  if (cand_cnt_) cudaFree(cand_cnt_);
+  if (cand_dist_) cudaFree(cand_dist_);
+  cand_ = nullptr;
+  cand_cnt_ = nullptr;
+  cand_dist_ = nullptr;
+  cand_rows_ = 0;
+  const size_t r = std::max<size_t>(rows, 1024);
+  ck(cudaMalloc(&cand_, r * kMaxCand * sizeof(int)), "cudaMalloc cand");
+  ck(cudaMalloc(&cand_cnt_, r * sizeof(int)), "cudaMalloc cand");
+  ck(cudaMalloc(&cand_dist_, r * kMaxCand * sizeof(float)), "cudaMalloc cand");
+  cand_rows_ = r;
+}
+
+void Session::ensure_embed(size_t nb) {
+  const size_t need = 2 * std::max<size_t>(nb, 1) * (size_t)st_.k;
+  if (need <= es_.cap_coo) return;
+  sync();
+  if (es_.coo_row) {
+    cudaFree(es_.coo_row);
+    cudaFree(es_.coo_col);
+    cudaFree(es_.coo_val);
+    cudaFree(es_.t_row);
+    cudaFree(es_.t_col);
+    cudaFree(es_.flag_tail);
+    cudaFree(es_.t_val);
+    cudaFree(es_.next_s);
+    cudaFree(es_.next_n);
+    cudaFree(es_.tmp2);
+    es_.coo_row = nullptr;
+  }
+  const size_t c = std::max(need, (size_t)4096);
+  ck(cudaMalloc(&es_.coo_row, c * sizeof(int)), "cudaMalloc coo");
+  ck(cudaMalloc(&es_.coo_col, c * sizeof(int)), "cudaMalloc coo");
+  ck(cudaMalloc(&es_.coo_val, c * sizeof(float)), "cudaMalloc coo");
+  ck(cudaMalloc(&es_.t_row, c * sizeof(int)), "cudaMalloc coo");
+  ck(cudaMalloc(&es_.t_col, c * sizeof(int)), "cudaMalloc coo");
+  ck(cudaMalloc(&es_.flag_tail, c * sizeof(int)), "cudaMalloc coo");
+  ck(cudaMalloc(&es_.t_val, c * sizeof(float)), "cudaMalloc coo");
+  ck(cudaMalloc(&es_.next_s, c * sizeof(float)), "cudaMalloc coo");
+  ck(cudaMalloc(&es_.next_n, c * sizeof(float)), "cudaMalloc coo");
+  ck(cudaMalloc(&es_.tmp2, (compact_tmp_ints((int)c) + 64) * sizeof(int)), "cudaMalloc coo");
+  es_.cap_coo = c;
+}
+
+// ---------------------------------------------------------------------------
+// statistics: CUDA events around the launches of interest
+// ---------------------------------------------------------------------------
+void Session::timed_begin(int slot) {
+  if (!stats_on_) return;
+  cudaEvent_t a, b;
+  if (ev_pool_.size() >= 2) {
+    a = ev_pool_.back();
+    ev_pool_.pop_back();
+    b = ev_pool_.back();
+    ev_pool_.pop_back();
+  } else {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+  }
+  cudaEventRecord(a, stream_);
+  ev_pending_.push_back({a, b, slot});
+}
+
+void Session::timed_end(int slot) {
+  if (!stats_on_ || ev_pending_.empty()) return;
+  (void)slot;
+  cudaEventRecord(ev_pending_.back().b, stream_);
+}
+
+void Session::collect_timings() {
+  if (ev_pending_.empty()) return;
+  for (auto &pr : ev_pending_) {
+    float ms = 0.0f;
+    if (cudaEventSynchronize(pr.b) == cudaSuccess && cudaEventElapsedTime(&ms, pr.a, pr.b) == cudaSuccess) {
+      if (pr.slot == 0) {
+        stats_.join_ms += ms;
+        stats_.join_launches += 1;
+      } else if (pr.slot == 1) {
+        stats_.cand_ms += ms;
+        stats_.cand_launches += 1;
+      } else if (pr.slot == 2) {
+        stats_.sgd_ms += ms;
+        stats_.sgd_launches += 1;
+      }
+    }
+    ev_pool_.push_back(pr.a);
+    ev_pool_.push_back(pr.b);
+  }
+  ev_pending_.clear();
+}
+
+void Session::reset_stats() {
+  sync();
+  collect_timings();
+  stats_ = gm_stats{};
+  cudaMemsetAsync(d_stat_, 0, 8 * sizeof(unsigned long long), stream_);
+  launch_counter_reset();
+  sync();
+}
+
+void Session::get_stats(gm_stats *out) {
+  sync();
+  collect_timings();
+  unsigned long long h[8];
+  ck(cudaMemcpy(h, d_stat_, sizeof(h), cudaMemcpyDeviceToHost), "stats");
+  stats_.join_nodes = h[0];
+  stats_.join_rows = h[1];
+  stats_.join_pairs = h[2];
+  stats_.join_merges = h[3];
+  stats_.cand_rows = h[4];
+  stats_.kernel_launches = launch_counter();
+  *out = stats_;
+}
+
+// ---------------------------------------------------------------------------
+// append (reference impl.cuh:77-101)
+// ---------------------------------------------------------------------------
+void Session::append(const float *rows, size_t n_rows, size_t n_cols, bool on_device) {
+  if (closed_) throw Error(GM_ERR_CLOSED, "session is closed");
+  if (n_rows == 0) return;
+  if (n_cols != p_.n_features)
+    throw Error(GM_ERR_RUNTIME, "n_features mismatch with numpy array second dimension.");
+  if (rows == nullptr) throw Error(GM_ERR_RUNTIME, "null input rows");
+  if (n_inserted_ + n_rows > p_.n_instances)
+    throw Error(GM_ERR_CAPACITY, "Exceeding maximum number of rows in storage");
+  float *dst = st_.X + n_inserted_ * (size_t)st_.ld;
+  ck(cudaMemcpy2DAsync(dst, (size_t)st_.ld * sizeof(float), rows, n_cols * sizeof(float),
+                       n_cols * sizeof(float), n_rows,
+                       on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream_),
+     "append copy");
+  n_inserted_ += n_rows;
+}
+
+// ---------------------------------------------------------------------------
+// run (reference impl.cuh:146-218)
+// ---------------------------------------------------------------------------
+gm_result Session::run(uint32_t n_ins, uint32_t n_upd, uint32_t n_emb) {
+  if (closed_) throw Error(GM_ERR_CLOSED, "session is closed");
+  gm_result r{};
+  log("[GPUMAP] run() start: insert=%u update=%u embed=%u inserted=%zu\n", n_ins, n_upd, n_emb,
+      n_inserted_);
+  if (!ins_done_) {
+    const auto t0 = Clock::now();
+    r.n_insertion_ops = insert(n_ins);
+    sync();
+    check_device_error("insertion");
+    const auto t1 = Clock::now();
+    r.insertion_time = std::chrono::duration<float>(t1 - t0).count();
+    ins_done_ = (ins_head_ == n_inserted_) && n_inserted_ == p_.n_instances;
+    log("[GPUMAP] insert done: actual=%u time=%.3fs\n", r.n_insertion_ops, r.insertion_time);
+  }
+  if (n_upd != 0 && !upd_done_) {
+    size_t changed = 0;
+    const auto t0 = Clock::now();
+    r.n_update_ops = update(n_upd, changed);
+    sync();
+    check_device_error("update");
+    const auto t1 = Clock::now();
+    r.n_update_changed_edges = changed;
+    r.update_time = std::chrono::duration<float>(t1 - t0).count();
+    log("[GPUMAP] update done: actual=%u changed_edges=%zu time=%.3fs\n", r.n_update_ops,
+        changed, r.update_time);
+  }
+  r.embedding_pending_edges = n_inserted_;
+  if (n_emb != 0 && n_inserted_ != 0 && !emb_done_) {
+    const auto t0 = Clock::now();
+    r.n_embedding_ops = embed(n_emb);
+    sync();
+    check_device_error("embedding");
+    const auto t1 = Clock::now();
+    r.embedding_time = std::chrono::duration<float>(t1 - t0).count();
+    log("[GPUMAP] embed done: actual=%u time=%.3fs\n", r.n_embedding_ops, r.embedding_time);
+  }
+  collect_timings();
+  stats_.phase_s[0] += r.insertion_time;
+  stats_.phase_s[1] += r.update_time;
+  stats_.phase_s[2] += r.embedding_time;
+  r.n_inserted_instances = n_inserted_;
+  r.insertion_queue_size = n_inserted_ - ins_head_;
+  r.update_queue_size = upd_q_.size();
+  r.embedding_queue_size = r.embedding_pending_edges;
+  r.insertion_completed = ins_done_;
+  r.update_completed = upd_done_;
+  r.embedding_completed = emb_done_;
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// insertion (reference impl.cuh:220-253, insertion_kernel.cuh:926-1095)
+// ---------------------------------------------------------------------------
+uint32_t Session::insert(uint32_t n_ops) {
+  const size_t qsize = n_inserted_ - ins_head_;
+  if (qsize == 0 || n_ops == 0) return 0;
+  const size_t B = std::min<size_t>(n_ops, qsize);
+  const int row0 = (int)ins_head_;
+  ins_head_ += B;
+  batch_hist_.push_back((uint32_t)row0);
+  if ((int)batch_hist_.size() > kWindowBatches) batch_hist_.pop_front();
+  const int window_start = (int)batch_hist_.front();
+  const int seed_i = (int)(n_ops * 9973u + (uint32_t)n_inserted_ * 7919u);
+  const uint64_t seed = (uint64_t)(int64_t)seed_i;
+  const int n = (int)n_inserted_;
+  const int nb = (int)B;
+  cudaStream_t s = stream_;
+
+  if (!bloom_clean_) {
+    ck(cudaMemsetAsync(st_.bloom, 0, (size_t)st_.n_cap * 64 * sizeof(uint32_t), s), "bloom");
+    bloom_clean_ = true;
+  }
+  ck(cudaMemsetAsync(st_.dirty, 0, (size_t)n * sizeof(int), s), "dirty");
+  ensure_cand(B);
+  launch_row_norms(st_, row0, nb, s);
+  launch_random_init(st_, row0, nb, n, window_start, seed, s);
+  for (int it = 0; it < kInsertIters; ++it) {
+    launch_sample_candidates(st_, row0, nb, n, cand_, cand_cnt_, s);
+    timed_begin(1);
+    launch_candidate_dists(st_, row0, nb, cand_, cand_cnt_, cand_dist_, s);
+    timed_end(1);
+    launch_forward_merge(st_, row0, nb, cand_, cand_cnt_, cand_dist_, s);
+    if (row0 > 0) launch_reverse_insert(st_, row0, nb, cand_, cand_cnt_, cand_dist_, s);
+  }
+  // existing rows whose list changed, ascending
+  compact_flags(st_.dirty, row0, -1, d_rows_, d_cnt_, d_tmp_, s);
+  launch_adopt_and_publish(st_, row0, nb, d_rows_, d_cnt_, row0, n, s);
+  launch_embed_init(st_, row0, nb, n, s);
+  ck(cudaMemcpyAsync(h_pin_, d_cnt_, sizeof(int), cudaMemcpyDeviceToHost, s), "count");
+  sync();
+  const int nd = (int)h_pin_[0];
+  if (nd > 0) {
+    ck(cudaMemcpyAsync(h_pin_, d_rows_, (size_t)nd * sizeof(int), cudaMemcpyDeviceToHost, s),
+       "rows");
+    sync();
+  }
+  // affected = batch rows then changed existing rows (insertion_kernel.cuh:1039-1089)
+  for (int i = 0; i < nb; ++i) upd_q_.push((uint32_t)(row0 + i));
+  for (int i = 0; i < nd; ++i) upd_q_.push(h_pin_[i]);
+  return (uint32_t)B;
+}
+
+// ---------------------------------------------------------------------------
+// update (reference impl.cuh:255-333)
+// ---------------------------------------------------------------------------
+uint32_t Session::update(uint32_t n_ops, size_t &changed) {
+  changed = 0;
+  const size_t n = n_inserted_;
+  if (n_ops == 0 || upd_done_ || n == 0) return 0;
+  const size_t threshold = (size_t)(0.0001f * (float)n);
+  uint32_t left = n_ops;
+  while (left > 0) {
+    std::vector<uint32_t> batch;
+    if ((size_t)left >= n) {
+      upd_q_.pop_n(upd_q_.size());
+      batch.resize(n);
+      std::iota(batch.begin(), batch.end(), 0u);
+    } else if ((size_t)left >= upd_q_.size()) {
+      batch = upd_q_.pop_n(upd_q_.size());
+      std::vector<char> seen(n, 0);
+      for (uint32_t v : batch) seen[v] = 1;
+      std::uniform_int_distribution<uint32_t> dist(0, (uint32_t)(n - 1));
+      uint32_t start = dist(rng_);
+      while (batch.size() < (size_t)left) {
+        const uint32_t c = (start++) % (uint32_t)n;
+        if (!seen[c]) {
+          seen[c] = 1;
+          batch.push_back(c);
+        }
+      }
+    } else {
+      batch = upd_q_.pop_n(left);
+    }
+    if (batch.empty()) break;
+    const size_t raw = batch.size();
+    std::vector<uint32_t> affected;
+    changed += update_round(batch, affected);
+    left -= (uint32_t)raw;
+    for (uint32_t v : affected) upd_q_.push(v);
+    if (upd_q_.size() < threshold) {
+      upd_done_ = (n == p_.n_instances);
+      break;
+    }
+  }
+  return n_ops - left;
+}
+
+// One UpdateAlgo::run (update_kernel.cuh:913-1054) on a batch.
+size_t Session::update_round(std::vector<uint32_t> &batch, std::vector<uint32_t> &affected) {
+  std::sort(batch.begin(), batch.end());
+  batch.erase(std::unique(batch.begin(), batch.end()), batch.end());
+  const int nb = (int)batch.size();
+  const int n = (int)n_inserted_;
+  cudaStream_t s = stream_;
+  std::memcpy(h_pin_, batch.data(), (size_t)nb * sizeof(uint32_t));
+  ck(cudaMemcpyAsync(d_batch_, h_pin_, (size_t)nb * sizeof(int), cudaMemcpyHostToDevice, s),
+     "batch");
+  ck(cudaMemsetAsync(us_.sizes, 0, (size_t)n * sizeof(int4), s), "sizes");
+  ck(cudaMemsetAsync(st_.dirty, 0, (size_t)n * sizeof(int), s), "dirty");
+  launch_sample_graph(st_, us_, d_batch_, nb, n, s);
+  bloom_clean_ = false;
+  build_reverse(st_, us_, d_batch_, nb, n, 0, d_tmp_, s);
+  build_reverse(st_, us_, d_batch_, nb, n, 1, d_tmp_, s);
+  launch_join_flags(us_, n, us_.hflag, s);
+  compact_flags(us_.hflag, n, -1, d_rows_, d_cnt_ + 3, d_tmp_, s);
+  timed_begin(0);
+  launch_local_join(st_, us_, d_rows_, d_cnt_ + 3, n, n, s);
+  timed_end(0);
+  compact_flags(st_.dirty, n, -1, d_rows2_, d_cnt_ + 0, d_tmp_, s);
+  ck(cudaMemsetAsync(d_cnt_ + 1, 0, sizeof(int), s), "edges");
+  launch_merge_publish(st_, us_, d_rows2_, d_cnt_ + 0, n, n, d_cnt_ + 1, us_.hflag, s);
+  compact_list(d_rows2_, d_cnt_ + 0, n, us_.hflag, d_rows_, d_cnt_ + 2, d_tmp_, s);
+  ck(cudaMemcpyAsync(h_pin_, d_cnt_, 4 * sizeof(int), cudaMemcpyDeviceToHost, s), "counts");
+  sync();
+  const int edges = (int)h_pin_[1];
+  const int na = (int)h_pin_[2];
+  if (na > 0) {
+    ck(cudaMemcpyAsync(h_pin_, d_rows_, (size_t)na * sizeof(int), cudaMemcpyDeviceToHost, s),
+       "affected");
+    sync();
+    affected.assign(h_pin_, h_pin_ + na);
+  }
+  return (size_t)edges;
+}
+
+// ---------------------------------------------------------------------------
+// embedding (reference impl.cuh:335-500)
+// ---------------------------------------------------------------------------
+uint32_t Session::embed(uint32_t n_ops) {
+  const size_t n = n_inserted_;
+  if (n_ops == 0 || n == 0) return 0;
+  const size_t total_n = p_.n_instances;
+  std::vector<uint32_t> batch;
+  if ((size_t)n_ops >= n) {
+    emb_new_head_ = n_inserted_;
+    batch.resize(n);
+    std::iota(batch.begin(), batch.end(), 0u);
+    emb_cursor_ = n - 1;
+    if (emb_cursor_ == total_n - 1 && upd_done_) ++sweeps_;
+  } else {
+    for (size_t v = emb_new_head_; v < n_inserted_; ++v) batch.push_back((uint32_t)v);
+    emb_new_head_ = n_inserted_;
+    size_t left = batch.size() >= (size_t)n_ops ? 0 : (size_t)n_ops - batch.size();
+    if (left > 0) {
+      std::vector<char> seen(n, 0);
+      for (uint32_t v : batch) seen[v] = 1;
+      size_t cursor = (emb_cursor_ == SIZE_MAX) ? 0 : (emb_cursor_ + 1) % n;
+      for (size_t checked = 0; left > 0 && checked < n; ++checked) {
+        if (!seen[cursor]) {
+          seen[cursor] = 1;
+          batch.push_back((uint32_t)cursor);
+          emb_cursor_ = cursor;
+          if (emb_cursor_ == total_n - 1 && upd_done_) ++sweeps_;
+          --left;
+        }
+        cursor = (cursor + 1) % n;
+      }
+    }
+  }
+  log("[GPUMAP] embed batch_size=%zu cursor=%zu\n", batch.size(), emb_cursor_);
+  const int nb = (int)batch.size();
+  const int ni = (int)n;
+  const int k = st_.k;
+  cudaStream_t s = stream_;
+  ensure_embed((size_t)nb);
+  std::memcpy(h_pin_, batch.data(), (size_t)nb * sizeof(uint32_t));
+  ck(cudaMemcpyAsync(d_batch_, h_pin_, (size_t)nb * sizeof(int), cudaMemcpyHostToDevice, s),
+     "batch");
+  const int euclid = p_.metric == GM_METRIC_EUCLIDEAN;
+  const double target = std::log2((double)(k - 1));
+  launch_fuzzy_graph(st_.pub_idx, st_.pub_dist, ni, k, euclid, d_batch_, nb, target, es_, s);
+  if (sweeps_ > 2) emb_done_ = upd_done_;
+  const uint64_t noise_seed = 42ull ^ (uint64_t)sweeps_;
+  launch_add_noise(st_.emb, ni, d_batch_, nb, 0.001f, noise_seed, es_, s);
+  timed_begin(2);
+  launch_optimize_layout(st_.emb, ni, nb, k, p_.alpha, 1.0f, p_.a, p_.b, (int)p_.max_epoch,
+                         (int)p_.negative_sample_rate, 42ull, es_, s);
+  timed_end(2);
+  const int nu = ni - nb;
+  if (nu > 0) {
+    ck(cudaMemsetAsync(es_.flag, 0, (size_t)ni * sizeof(int), s), "flags");
+    launch_mark_rows(d_batch_, nb, es_.flag, s);
+    compact_flags(es_.flag, ni, 0, es_.unsel, d_cnt_ + 4, d_tmp_, s);
+    launch_heuristic(st_.pub_idx, st_.pub_dist, ni, k, euclid, es_.unsel, nu, st_.emb, es_, s);
+  }
+  return (uint32_t)nb;
+}
+
+void Session::close() {
+  if (closed_) return;
+  cudaStreamSynchronize(stream_);
+  closed_ = true;
+}
+
+void Session::debug_scalars(int64_t *out, int cnt) const {
+  int iscal[16] = {0};
+  unsigned err = 0;
+  cudaStreamSynchronize(stream_);
+  cudaMemcpy(iscal, es_.iscal, sizeof(iscal), cudaMemcpyDeviceToHost);
+  cudaMemcpy(&err, st_.err, sizeof(err), cudaMemcpyDeviceToHost);
+  int64_t v[11] = {(int64_t)n_inserted_,
+                   (int64_t)ins_head_,
+                   (int64_t)emb_new_head_,
+                   emb_cursor_ == SIZE_MAX ? -1 : (int64_t)emb_cursor_,
+                   (int64_t)sweeps_,
+                   iscal[0],
+                   iscal[1],
+                   iscal[2],
+                   iscal[3],
+                   (int64_t)upd_q_.size(),
+                   (int64_t)err};
+  for (int i = 0; i < cnt && i < 11; ++i) out[i] = v[i];
+}
+
+}  // namespace gm

@@ -1,0 +1,535 @@
+// Embedding phase: fuzzy simplicial set over the published k-NN (self
+// prepended), edge scheduling and negative-sampling SGD.  Restates the
+// reference's embedding_kernel.cuh and Impl::embed (impl.cuh:335-500) with
+// every count and threshold kept on the device (no host round trips).
+#include "gm_common.cuh"
+#include "gm_kernels.h"
+
+namespace gm {
+
+// Scalar slots in EmbedScratch.
+//   fscal: 0 mean_dist, 1 max_w, 2 rounding, 3 x_min, 4 x_max
+//   iscal: 0 nnz (directed + extras), 1 extras, 2 nnz after trim, 3 max degree
+enum { FS_MEAN = 0, FS_MAXW = 1, FS_ROUND = 2, FS_XMIN = 3, FS_XMAX = 4 };
+enum { IS_NNZ = 0, IS_EXTRA = 1, IS_NNZ2 = 2, IS_MAXDEG = 3 };
+
+namespace {
+
+constexpr float kSmoothTol = 1e-5f;  // SMOOTH_K_TOLERANCE
+constexpr float kMinKDistScale = 1e-3f;
+
+// Embed-time k-NN (reference prepend_self_knn_kernel, embedding_kernel.cuh:599-631):
+// column 0 is the row itself at distance 0; column c >= 1 is published
+// neighbour c-1 (the k-th is dropped); euclidean distances are square-rooted.
+GM_D uint32_t eidx(const uint32_t *pub_idx, int k, int row, int c) {
+  return c == 0 ? (uint32_t)row : pub_idx[(size_t)row * (k + 1) + (c - 1)];
+}
+GM_D float edist(const float *pub_dist, int k, int row, int c, int euclid) {
+  if (c == 0) return 0.0f;
+  const float v = pub_dist[(size_t)row * (k + 1) + (c - 1)];
+  return euclid ? __fsqrt_rn(v > 0.0f ? v : 0.0f) : v;
+}
+GM_D bool valid_d(float v) { return isfinite(v) && v >= 0.0f && v < FLT_MAX / 2.0f; }
+
+GM_D float membership(float dist, float rho, float sigma) {
+  const float dr = __fsub_rn(dist, rho);
+  if (dr <= 0.0f || sigma == 0.0f) return 1.0f;
+  const float v = gm_expf(-__fdiv_rn(dr, sigma));
+  return v < FLT_MIN ? FLT_MIN : v;
+}
+
+// Block sums of the embed-time distances (256 per block, FP32 tree).
+__global__ void k_mean_partial(const float *pub_dist, int n, int k, int euclid,
+                               float *part, int *ipart) {
+  __shared__ float ss[256];
+  __shared__ float sc[256];
+  const int t = threadIdx.x;
+  const long g = (long)blockIdx.x * 256 + t;
+  float v = 0.0f, c = 0.0f;
+  if (g < (long)n * k) {
+    const int row = (int)(g / k), ki = (int)(g % k);
+    const float raw = edist(pub_dist, k, row, ki, euclid);
+    if (raw >= 0.0f && raw < FLT_MAX / 2.0f) {
+      v = raw;
+      c = 1.0f;
+    }
+  }
+  ss[t] = v;
+  sc[t] = c;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (t < s) {
+      ss[t] = __fadd_rn(ss[t], ss[t + s]);
+      sc[t] = __fadd_rn(sc[t], sc[t + s]);
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    part[blockIdx.x] = ss[0];
+    ipart[blockIdx.x] = (int)sc[0];
+  }
+}
+
+__global__ void k_mean_final(const float *part, const int *ipart, int nb, float *fscal) {
+  float s = 0.0f;
+  long c = 0;
+  for (int i = 0; i < nb; ++i) {
+    s = __fadd_rn(s, part[i]);
+    c += ipart[i];
+  }
+  fscal[FS_MEAN] = (c > 0 && isfinite(s) && s > 0.0f) ? __fdiv_rn(s, (float)c) : 1.0f;
+}
+
+// sigma / rho per row, one warp per row; the bisection's target sum is
+// accumulated in FP64 by a fixed butterfly (reference smooth_knn_dist_kernel,
+// embedding_kernel.cuh:135-207).
+__global__ void k_smooth_knn(const float *pub_dist, int n, int k, int euclid,
+                             const float *fscal, double target, float *sigma,
+                             float *rho) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const int row = warp;
+  const float raw = (lane < k) ? edist(pub_dist, k, row, lane, euclid) : 0.0f;
+  const float san = (lane < k && valid_d(raw)) ? raw : 0.0f;
+  float sum = 0.0f;
+  for (int c = 0; c < k; ++c) sum = __fadd_rn(sum, __shfl_sync(0xffffffffu, san, c));
+  const unsigned nz = __ballot_sync(0xffffffffu, lane < k && san > 0.0f);
+  const float mean_dist = fscal[FS_MEAN];
+  if (nz == 0u) {
+    if (lane == 0) {
+      rho[row] = 0.0f;
+      sigma[row] = __fmul_rn(kMinKDistScale, mean_dist);
+    }
+    return;
+  }
+  const int start_nz = __ffs(nz) - 1;
+  const float row_mean = __fdiv_rn(sum, (float)k);
+  const float r = __shfl_sync(0xffffffffu, raw, start_nz);
+  float lo = 0.0f, hi = FLT_MAX, mid = 1.0f;
+  const bool contrib = (lane >= 2 && lane < k);
+  const float dj = __fsub_rn(san, r);
+  for (int it = 0; it < 64; ++it) {
+    double term = 0.0;
+    if (contrib) term = (dj > 0.0f) ? (double)gm_expf(__fdiv_rn(-dj, mid)) : 1.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
+    const double psum = term;
+    if (fabs(psum - target) < (double)kSmoothTol) break;
+    if (psum > target) {
+      hi = mid;
+      mid = __fmul_rn(__fadd_rn(lo, hi), 0.5f);
+    } else {
+      lo = mid;
+      mid = (hi == FLT_MAX) ? __fmul_rn(mid, 2.0f) : __fmul_rn(__fadd_rn(lo, hi), 0.5f);
+    }
+  }
+  if (!isfinite(mid) || mid <= 0.0f) mid = 1.0f;
+  const float min_scale = __fmul_rn(kMinKDistScale, (r > 0.0f) ? row_mean : mean_dist);
+  if (lane == 0) {
+    rho[row] = r;
+    sigma[row] = mid < min_scale ? min_scale : mid;
+  }
+}
+
+// Directed membership p_ij for batch rows and the fuzzy union
+// w = p_ij + p_ji - p_ij p_ji; flag marks edges whose reverse is absent
+// (reference: embedding_kernel.cuh:214-320).
+__global__ void k_memb_sym(const uint32_t *pub_idx, const float *pub_dist, int n, int k,
+                           int euclid, const float *sigma, const float *rho,
+                           const int *batch, int nb, int *coo_row, int *coo_col,
+                           float *coo_val, int *flag) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= nb * k) return;
+  const int bi = tid / k, ki = tid - bi * k;
+  const int row = batch[bi];
+  const uint32_t raw_col = eidx(pub_idx, k, row, ki);
+  const bool valid_col = raw_col < (uint32_t)n;
+  const int col = valid_col ? (int)raw_col : row;
+  const float dist = edist(pub_dist, k, row, ki, euclid);
+  float pij = 0.0f;
+  if (valid_col && col != row && valid_d(dist)) pij = membership(dist, rho[row], sigma[row]);
+  const int i = row, j = col;
+  float pji = 0.0f;
+  for (int kj = 0; kj < k; ++kj) {
+    if ((int)eidx(pub_idx, k, j, kj) == i) {
+      const float dji = edist(pub_dist, k, j, kj, euclid);
+      if (!valid_d(dji)) break;
+      pji = membership(dji, rho[j], sigma[j]);
+      break;
+    }
+  }
+  const float w = __fmaf_rn(-pij, pji, __fadd_rn(pij, pji));
+  coo_row[tid] = i;
+  coo_col[tid] = j;
+  coo_val[tid] = w;
+  flag[tid] = (pji == 0.0f) ? 1 : 0;
+}
+
+__global__ void k_write_extras(const int *idx, const int *cnt, int ndir, int *coo_row,
+                               int *coo_col, float *coo_val, int *iscal) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = *cnt;
+  if (q == 0) {
+    iscal[IS_NNZ] = ndir + c;
+    iscal[IS_EXTRA] = c;
+  }
+  if (q >= c) return;
+  const int src = idx[q];
+  coo_row[ndir + q] = coo_col[src];
+  coo_col[ndir + q] = coo_row[src];
+  coo_val[ndir + q] = coo_val[src];
+}
+
+// max_w over non-negative weights via the int ordering of their bits.
+__global__ void k_max_w(const float *vals, const int *iscal, float *fscal) {
+  const int nnz = iscal[IS_NNZ];
+  float m = 0.0f;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += gridDim.x * blockDim.x)
+    m = fmaxf(m, vals[q]);
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0f)
+    atomicMax(reinterpret_cast<int *>(&fscal[FS_MAXW]), __float_as_int(m));
+}
+
+// Trim flag: keep w >= max_w / n_epochs (reference trim_graph, :348-400).
+__global__ void k_trim_flags(const float *vals, const int *iscal, const float *fscal,
+                             int n_epochs, int *flag, int nmax) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nmax) return;
+  const int nnz = iscal[IS_NNZ];
+  const float mw = fscal[FS_MAXW];
+  int keep = 0;
+  if (q < nnz && mw > 0.0f) keep = vals[q] >= __fdiv_rn(mw, (float)n_epochs) ? 1 : 0;
+  flag[q] = keep;
+}
+
+// Gather survivors; epochs_per_sample; head degrees; epoch state
+// (reference: :469-495, :405-460).
+__global__ void k_gather_sched(const int *idx, const int *iscal, const int *crow,
+                               const int *ccol, const float *cval, const float *fscal,
+                               int n_epochs, float nsr_inv, int *trow, int *tcol,
+                               float *eps, float *next_s, float *next_n, int *deg) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= iscal[IS_NNZ2]) return;
+  const int src = idx[q];
+  const float mw = fscal[FS_MAXW];
+  const float w = cval[src];
+  const float ns = __fmul_rn((float)n_epochs, __fdiv_rn(w, mw));
+  const float e = (ns > 0.0f) ? __fdiv_rn((float)n_epochs, ns) : -1.0f;
+  trow[q] = crow[src];
+  tcol[q] = ccol[src];
+  eps[q] = e;
+  next_s[q] = e;
+  next_n[q] = __fmul_rn(e, nsr_inv);
+  atomicAdd(&deg[crow[src]], 1);
+}
+
+__global__ void k_max_deg(const int *deg, int n, int *iscal) {
+  int m = 0;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+    m = max(m, deg[q]);
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(&iscal[IS_MAXDEG], m);
+}
+
+// Gradient rounding factor 2^ceil-ish via frexp (reference :433-460).
+__global__ void k_rounding(int *iscal, float *fscal, float alpha) {
+  const int nnz = iscal[IS_NNZ2];
+  const int md = iscal[IS_MAXDEG];
+  float r = 1.0f;
+  if (nnz > 0 && md > 0) {
+    const float max_abs = __fmul_rn(__fmul_rn((float)md, 4.0f), fabsf(alpha));
+    const float denom = __fsub_rn(1.0f, __fmul_rn(__fmul_rn(2.0f, (float)md), FLT_EPSILON));
+    const float delta = __fdiv_rn(max_abs, denom);
+    int ex;
+    frexpf(delta, &ex);
+    r = ldexpf(1.0f, ex);
+  }
+  fscal[FS_ROUND] = r;
+}
+
+GM_D float fclip(float v) {
+  if (!isfinite(v)) return 0.0f;
+  return fmaxf(fminf(v, 4.0f), -4.0f);
+}
+GM_D float trunc_grad(float rounding, float x) {
+  return __fsub_rn(__fadd_rn(rounding, x), rounding);
+}
+
+// One SGD epoch (reference optimize_batch_kernel, :509-589; Hogwild
+// updates, tail moved by rounded atomics, head accumulated then added).
+__global__ void k_sgd_epoch(float *emb, const int *head, const int *tail,
+                            const int *iscal, int n, const float *eps, float *next_s,
+                            float *next_n, float alpha, int epoch, float gamma, float a,
+                            float b, float nsr_inv, uint64_t seed, const float *fscal) {
+  const int nnz = iscal[IS_NNZ2];
+  const float rounding = fscal[FS_ROUND];
+  const float fe = (float)epoch;
+  const float bm1 = __fsub_rn(b, 1.0f);
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < nnz;
+       row += gridDim.x * blockDim.x) {
+    const float ns = next_s[row];
+    if (ns > fe) continue;
+    const float ep = eps[row];
+    const float ep_neg = __fmul_rn(ep, nsr_inv);
+    const int j = head[row], kk = tail[row];
+    float *cp = emb + (size_t)j * 2;
+    float *op = emb + (size_t)kk * 2;
+    float cur0 = cp[0], cur1 = cp[1];
+    const float o0 = op[0], o1 = op[1];
+    const float dx = __fsub_rn(cur0, o0), dy = __fsub_rn(cur1, o1);
+    const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+    float attr = 0.0f;
+    if (d2 > 0.0f)
+      attr = __fdiv_rn(__fmul_rn(__fmul_rn(-2.0f, __fmul_rn(a, b)), gm_powf(d2, bm1)),
+                       __fadd_rn(__fmul_rn(a, gm_powf(d2, b)), 1.0f));
+    float g0 = __fmul_rn(fclip(__fmul_rn(attr, dx)), alpha);
+    float g1 = __fmul_rn(fclip(__fmul_rn(attr, dy)), alpha);
+    cur0 = __fadd_rn(cur0, g0);
+    cur1 = __fadd_rn(cur1, g1);
+    atomicAdd(op, trunc_grad(rounding, -g0));
+    atomicAdd(op + 1, trunc_grad(rounding, -g1));
+    next_s[row] = __fadd_rn(ns, ep);
+    const float nn = next_n[row];
+    const int n_neg = (int)__fdiv_rn(__fsub_rn(fe, nn), ep_neg);
+    if (n_neg > 0) {
+      Philox g;
+      philox_init(g, seed, (uint32_t)row, kTagNegSample);
+      for (int p = 0; p < n_neg; ++p) {
+        const int r = (int)(philox_next(g) % (uint32_t)n);
+        if (r == j) continue;
+        const float q0 = emb[(size_t)r * 2], q1 = emb[(size_t)r * 2 + 1];
+        const float ex = __fsub_rn(cur0, q0), ey = __fsub_rn(cur1, q1);
+        const float d2n = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+        float rep = 0.0f;
+        if (d2n > 0.0f)
+          rep = __fdiv_rn(__fmul_rn(__fmul_rn(2.0f, gamma), b),
+                          __fmul_rn(__fadd_rn(0.001f, d2n),
+                                    __fadd_rn(__fmul_rn(a, gm_powf(d2n, b)), 1.0f)));
+        const float h0 = (rep > 0.0f) ? __fmul_rn(fclip(__fmul_rn(rep, ex)), alpha)
+                                      : __fmul_rn(4.0f, alpha);
+        const float h1 = (rep > 0.0f) ? __fmul_rn(fclip(__fmul_rn(rep, ey)), alpha)
+                                      : __fmul_rn(4.0f, alpha);
+        cur0 = __fadd_rn(cur0, h0);
+        cur1 = __fadd_rn(cur1, h1);
+        g0 = __fadd_rn(g0, h0);
+        g1 = __fadd_rn(g1, h1);
+      }
+      next_n[row] = __fadd_rn(nn, __fmul_rn((float)n_neg, ep_neg));
+    }
+    atomicAdd(cp, trunc_grad(rounding, g0));
+    atomicAdd(cp + 1, trunc_grad(rounding, g1));
+  }
+}
+
+__global__ void k_epoch_init(const float *eps, int nnz, float nsr_inv, float *next_s,
+                             float *next_n) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nnz) return;
+  next_s[q] = eps[q];
+  next_n[q] = __fmul_rn(eps[q], nsr_inv);
+}
+
+// x-range of the embedding (first component) for the noise scale.
+__global__ void k_xrange_partial(const float *emb, int n, float *part) {
+  __shared__ float smin[256], smax[256];
+  const int t = threadIdx.x;
+  float mn = FLT_MAX, mx = -FLT_MAX;
+  for (int i = blockIdx.x * 256 + t; i < n; i += gridDim.x * 256) {
+    const float v = emb[(size_t)i * 2];
+    mn = fminf(mn, v);
+    mx = fmaxf(mx, v);
+  }
+  smin[t] = mn;
+  smax[t] = mx;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (t < s) {
+      smin[t] = fminf(smin[t], smin[t + s]);
+      smax[t] = fmaxf(smax[t], smax[t + s]);
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    part[2 * blockIdx.x] = smin[0];
+    part[2 * blockIdx.x + 1] = smax[0];
+  }
+}
+
+__global__ void k_add_noise(float *emb, const int *batch, int nb, const float *part,
+                            int nparts, float noise_scale, uint64_t seed) {
+  __shared__ float s_scale;
+  if (threadIdx.x == 0) {
+    float mn = FLT_MAX, mx = -FLT_MAX;
+    for (int i = 0; i < nparts; ++i) {
+      mn = fminf(mn, part[2 * i]);
+      mx = fmaxf(mx, part[2 * i + 1]);
+    }
+    s_scale = __fmul_rn(noise_scale, __fsub_rn(mx, mn));
+  }
+  __syncthreads();
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= nb * 2) return;
+  const int node = batch[tid >> 1], comp = tid & 1;
+  Philox g;
+  philox_init(g, seed, (uint32_t)tid, kTagNoise);
+  const float z = gm_normal(g);
+  float *p = emb + (size_t)node * 2 + comp;
+  *p = __fadd_rn(*p, __fmul_rn(z, s_scale));
+}
+
+// Rows not selected this round move to the membership-weighted mean of their
+// neighbours' positions, read from a snapshot (reference :811-894).  Ids
+// outside [0, n) are skipped.
+__global__ void k_heuristic(const uint32_t *pub_idx, const float *pub_dist, int n, int k,
+                            int euclid, const float *sigma, const float *rho,
+                            const int *unsel, int nu, const float *snap, float *emb) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nu) return;
+  const int row = unsel[q];
+  const float sg = sigma[row], rh = rho[row];
+  float wsum = 0.0f, a0 = 0.0f, a1 = 0.0f;
+  for (int ki = 0; ki < k; ++ki) {
+    const int col = (int)eidx(pub_idx, k, row, ki);
+    if (col == row) continue;
+    const float dist = edist(pub_dist, k, row, ki, euclid);
+    if (!valid_d(dist)) continue;
+    if (col < 0 || col >= n) continue;
+    const float w = membership(dist, rh, sg);
+    wsum = __fadd_rn(wsum, w);
+    a0 = __fmaf_rn(w, snap[(size_t)col * 2], a0);
+    a1 = __fmaf_rn(w, snap[(size_t)col * 2 + 1], a1);
+  }
+  if (wsum > 0.0f) {
+    emb[(size_t)row * 2] = __fdiv_rn(a0, wsum);
+    emb[(size_t)row * 2 + 1] = __fdiv_rn(a1, wsum);
+  }
+}
+
+__global__ void k_mark_rows(const int *rows, int nr, int *flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nr) flag[rows[i]] = 1;
+}
+
+inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace
+
+void launch_mark_rows(const int *rows, int nr, int *flag, cudaStream_t s) {
+  if (nr <= 0) return;
+  k_mark_rows<<<cdiv(nr, 256), 256, 0, s>>>(rows, nr, flag);
+  note_launch();
+}
+
+void launch_fuzzy_graph(const uint32_t *pub_idx, const float *pub_dist, int n, int k,
+                        int euclidean, const int *batch, int nb, double log2_target,
+                        EmbedScratch &e, cudaStream_t s) {
+  const long total = (long)n * k;
+  const int nbl = cdiv(total, 256);
+  k_mean_partial<<<nbl, 256, 0, s>>>(pub_dist, n, k, euclidean, e.partial, e.ipartial);
+  note_launch();
+  k_mean_final<<<1, 1, 0, s>>>(e.partial, e.ipartial, nbl, e.fscal);
+  note_launch();
+  k_smooth_knn<<<cdiv((long)n * 32, 256), 256, 0, s>>>(pub_dist, n, k, euclidean, e.fscal,
+                                                       log2_target, e.sigma, e.rho);
+  note_launch();
+  const int ndir = nb * k;
+  if (ndir > 0)
+    k_memb_sym<<<cdiv(ndir, 256), 256, 0, s>>>(pub_idx, pub_dist, n, k, euclidean, e.sigma,
+                                               e.rho, batch, nb, e.coo_row, e.coo_col,
+                                               e.coo_val, e.t_row);
+    note_launch();
+  compact_flags(e.t_row, ndir, -1, e.t_col, e.iscal + IS_EXTRA, e.tmp2, s);
+  k_write_extras<<<cdiv(ndir > 0 ? ndir : 1, 256), 256, 0, s>>>(
+      e.t_col, e.iscal + IS_EXTRA, ndir, e.coo_row, e.coo_col, e.coo_val, e.iscal);
+  note_launch();
+}
+
+void launch_schedule(int n, int nb, int k, float alpha0, int n_epochs, int neg_rate,
+                     EmbedScratch &e, cudaStream_t s) {
+  if (n <= 0 || n_epochs <= 0 || nb <= 0) {
+    cudaMemsetAsync(e.iscal + IS_NNZ2, 0, sizeof(int), s);
+    return;
+  }
+  const int nmax = 2 * nb * k;
+  cudaMemsetAsync(e.fscal + FS_MAXW, 0, sizeof(float), s);
+  cudaMemsetAsync(e.iscal + IS_MAXDEG, 0, sizeof(int), s);
+  cudaMemsetAsync(e.deg, 0, sizeof(int) * (size_t)n, s);
+  k_max_w<<<min(cdiv(nmax, 256), 1024), 256, 0, s>>>(e.coo_val, e.iscal, e.fscal);
+  note_launch();
+  k_trim_flags<<<cdiv(nmax, 256), 256, 0, s>>>(e.coo_val, e.iscal, e.fscal, n_epochs,
+                                               e.t_row, nmax);
+  note_launch();
+  compact_flags_dev(e.t_row, e.iscal + IS_NNZ, nmax, e.t_col, e.iscal + IS_NNZ2, e.tmp2, s);
+  // t_col holds survivor indices; gather into (t_row, flag_tail, t_val)
+  const float nsr_inv = 1.0f / (float)neg_rate;  // inf when 0: no negatives
+  k_gather_sched<<<cdiv(nmax, 256), 256, 0, s>>>(e.t_col, e.iscal, e.coo_row, e.coo_col,
+                                                 e.coo_val, e.fscal, n_epochs, nsr_inv,
+                                                 e.t_row, e.flag_tail, e.t_val, e.next_s,
+                                                 e.next_n, e.deg);
+  note_launch();
+  k_max_deg<<<min(cdiv(n, 256), 1024), 256, 0, s>>>(e.deg, n, e.iscal);
+  note_launch();
+  k_rounding<<<1, 1, 0, s>>>(e.iscal, e.fscal, alpha0);
+  note_launch();
+}
+
+void launch_optimize_layout(float *emb, int n, int nb, int k, float alpha0, float gamma,
+                            float a, float b, int n_epochs, int neg_rate, uint64_t seed,
+                            EmbedScratch &e, cudaStream_t s) {
+  launch_schedule(n, nb, k, alpha0, n_epochs, neg_rate, e, s);
+  if (n <= 0 || n_epochs <= 0 || nb <= 0) return;
+  launch_sgd(emb, n, e.t_row, e.flag_tail, e.t_val, e.next_s, e.next_n, e.iscal, e.fscal,
+             2 * nb * k, alpha0, gamma, a, b, n_epochs, neg_rate, seed, s);
+}
+
+void launch_epoch_init(const float *eps, int nnz, int neg_rate, float *next_s,
+                       float *next_n, cudaStream_t s) {
+  if (nnz <= 0) return;
+  k_epoch_init<<<cdiv(nnz, 256), 256, 0, s>>>(eps, nnz, 1.0f / (float)neg_rate, next_s,
+                                              next_n);
+  note_launch();
+}
+
+void launch_sgd(float *emb, int n, const int *head, const int *tail, const float *eps,
+                float *next_s, float *next_n, const int *iscal, const float *fscal,
+                int nnz_max, float alpha0, float gamma, float a, float b, int n_epochs,
+                int neg_rate, uint64_t seed, cudaStream_t s) {
+  if (n <= 0 || n_epochs <= 0 || nnz_max <= 0) return;
+  const float nsr_inv = 1.0f / (float)neg_rate;
+  const int grid = cdiv(nnz_max, 256);
+  float alpha = alpha0;
+  uint64_t cur_seed = seed;
+  for (int ep = 0; ep < n_epochs; ++ep) {
+    k_sgd_epoch<<<grid, 256, 0, s>>>(emb, head, tail, iscal, n, eps, next_s, next_n, alpha,
+                                     ep, gamma, a, b, nsr_inv, cur_seed, fscal);
+    note_launch();
+    // alpha and seed for the next epoch (reference embedding_kernel.cuh:790-792)
+    alpha = alpha0 * (1.0f - (float)ep / (float)n_epochs);
+    cur_seed += 1;
+  }
+}
+
+void launch_add_noise(float *emb, int n, const int *batch, int nb, float noise_scale,
+                      uint64_t seed, EmbedScratch &e, cudaStream_t s) {
+  if (nb <= 0 || noise_scale == 0.0f || n <= 0) return;
+  const int nparts = min(cdiv(n, 256), 256);
+  k_xrange_partial<<<nparts, 256, 0, s>>>(emb, n, e.partial);
+  note_launch();
+  k_add_noise<<<cdiv(nb * 2, 256), 256, 0, s>>>(emb, batch, nb, e.partial, nparts,
+                                                noise_scale, seed);
+  note_launch();
+}
+
+void launch_heuristic(const uint32_t *pub_idx, const float *pub_dist, int n, int k,
+                      int euclidean, const int *unsel, int nu, float *emb,
+                      EmbedScratch &e, cudaStream_t s) {
+  if (nu <= 0 || n <= 0 || k <= 0) return;
+  cudaMemcpyAsync(e.snap, emb, sizeof(float) * 2 * (size_t)n, cudaMemcpyDeviceToDevice, s);
+  k_heuristic<<<cdiv(nu, 128), 128, 0, s>>>(pub_idx, pub_dist, n, k, euclidean, e.sigma,
+                                            e.rho, unsel, nu, e.snap, emb);
+  note_launch();
+}
+
+}  // namespace gm

@@ -1,0 +1,105 @@
+"""Pins against outputs of the reference itself (fixtures in tests/golden,
+regenerated by tests/golden/make_golden.py from the reference tree)."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def test_queue_rules_match_reference_queue_cuh(oracle_mod):
+    # output of the reference's own cpp/src/queue.cuh on a fixed script
+    assert oracle_mod.queue_script() == (GOLD / "queue_golden.txt").read_text()
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return json.loads((GOLD / "schedule_golden.json").read_text())
+
+
+class _R:
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+
+def _drive(st, script):
+    np.random.seed(1234)
+    out = []
+    for res in script:
+        for tl in (0.5, 2.0, 10.0):
+            out.append([int(v) for v in st.allocate(tl)])
+        r = _R(**res)
+        st.update(r)
+        for name, flag in (("insertion", r.insertion_completed), ("update", r.update_completed),
+                           ("embedding", r.embedding_completed)):
+            if flag:
+                st.on_operation_complete(name)
+        out.append([float(x) for x in st.get_progress()])
+    return out
+
+
+def test_weighted_strategy_matches_reference(gold):
+    from gpumap_gb300.schedule import WeightedStrategy
+
+    assert _drive(WeightedStrategy(n_instances=70000, n_neighbors=15), gold["script"]) == gold["weighted"]
+
+
+def test_weighted_linear_matches_reference(gold):
+    from gpumap_gb300.schedule import DefaultLinearEstimator, WeightedStrategy
+
+    st = WeightedStrategy(n_instances=70000, insertion_estimator=DefaultLinearEstimator(),
+                          update_estimator=DefaultLinearEstimator(), embedding_estimator=DefaultLinearEstimator())
+    assert _drive(st, gold["script"]) == gold["weighted_linear"]
+
+
+def test_sequential_strategy_matches_reference(gold):
+    from gpumap_gb300.schedule import SequentialPriorityStrategy
+
+    assert _drive(SequentialPriorityStrategy(n_instances=70000), gold["script"]) == gold["sequential"]
+
+
+@pytest.mark.parametrize("kind", ["mean_rate", "linear"])
+def test_estimators_match_reference(gold, kind):
+    from gpumap_gb300.schedule import DefaultLinearEstimator, MeanRateEstimator
+
+    est = MeanRateEstimator() if kind == "mean_rate" else DefaultLinearEstimator()
+    out = []
+    for res in gold["script"]:
+        est.add_sample(res["n_update_ops"], res["update_time"])
+        row = []
+        for budget in (0.0, 0.3, 1.0, 5.0):
+            try:
+                row.append(int(est.estimate_ops(budget, 0.95)))
+            except ValueError:
+                row.append(None)
+        try:
+            row.append(float(est.predict_time(1000, 0.9)))
+        except ValueError:
+            row.append(None)
+        out.append(row)
+    assert out == gold[kind]
+
+
+def test_find_ab_params_matches_reference(gold):
+    from gpumap_gb300.gpumap import find_ab_params
+
+    for md, (a, b) in gold["ab_params"].items():
+        ga, gb = find_ab_params(1.0, float(md))
+        assert abs(ga - a) <= 1e-9 * max(1.0, abs(a)) and abs(gb - b) <= 1e-9 * max(1.0, abs(b))
+
+
+def test_persistent_estimator_roundtrip(tmp_path):
+    from gpumap_gb300.schedule import MeanRateEstimator, PersistentEstimator
+
+    db = tmp_path / "est" / "h.sqlite"
+    p = PersistentEstimator(MeanRateEstimator(), str(db), "update")
+    for ops, t in ((1000, 0.5), (2000, 1.1), (1500, 0.7)):
+        p.add_sample(ops, t)
+    p.log_run("x", 8, 100)
+    ref = p.estimate_ops(2.0)
+    p.close()
+    q = PersistentEstimator(MeanRateEstimator(), str(db), "update")
+    assert q.estimate_ops(2.0) == ref
+    q.close()

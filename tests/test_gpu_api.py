@@ -1,0 +1,90 @@
+"""The Python surface (gpumap_gb300.GPUMAP over the pybind11 module) on the GPU."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _model(n=3000, d=16, k=15, seed=0, **kw):
+    import gpumap_gb300 as gm
+    from gpumap_gb300.data_loader import ArrayDataLoader
+    from gpumap_gb300.datasets import gaussian_mixture
+
+    X, _ = gaussian_mixture(n, d, seed=seed)
+    p = gm.GPUMAPParams()
+    p.n_instances, p.n_features, p.n_neighbors = n, d, k
+    p.max_epoch = 50
+    for key, v in kw.items():
+        setattr(p, key, v)
+    return X, gm.GPUMAP(ArrayDataLoader(X), p)
+
+
+def test_run_with_n_ops_views():
+    import torch
+
+    X, m = _model()
+    res = None
+    for _ in range(6):
+        res = m.run_with_n_ops(500, 1500, 800)
+    assert res.n_inserted_instances == 3000 and res.insertion_completed
+    assert m.n_inserted_instances == 3000
+    emb, idx, dst = m.get_embedding(), m.get_neighbor_indices(), m.get_neighbor_dists()
+    assert tuple(emb.shape) == (3000, 2) and tuple(idx.shape) == (3000, 15) and tuple(dst.shape) == (3000, 15)
+    assert isinstance(emb, torch.Tensor) and emb.is_cuda
+    assert torch.isfinite(emb).all()
+    i64 = idx.to(torch.int64).cpu().numpy()
+    assert np.all((i64 >= 0) & (i64 < 3000))
+    # dists are squared L2 of the listed ids
+    d2 = ((X[:, None, :].astype(np.float64) - X[i64].astype(np.float64)) ** 2).sum(-1)
+    assert np.max(np.abs(dst.cpu().numpy() - d2) / np.maximum(d2, 1e-3)) < 1e-4
+    m.close()
+
+
+def test_run_with_target_latency_and_strategy():
+    import gpumap_gb300 as gm
+    from gpumap_gb300.data_loader import ArrayDataLoader
+    from gpumap_gb300.datasets import gaussian_mixture
+
+    X, _ = gaussian_mixture(4000, 8, seed=2)
+    p = gm.GPUMAPParams()
+    p.n_instances, p.n_features = 4000, 8
+    p.max_epoch = 20
+    m = gm.GPUMAP(ArrayDataLoader(X), p, strategy=gm.SequentialPriorityStrategy(n_instances=4000))
+    res = m.run(0.5)
+    assert res.n_inserted_instances == 4000 and res.insertion_completed  # whole budget to insertion
+    res = m.run(0.5)
+    assert res.n_update_ops > 0 and res.n_insertion_ops == 0
+    m.close()
+    m2 = gm.GPUMAP(ArrayDataLoader(X), p)
+    for _ in range(3):
+        r = m2.run(0.2)
+        assert r.n_insertion_ops >= min(500, 4000)
+    assert 0.0 < m2.strategy.get_progress()[0] <= 1.0
+    m2.close()
+
+
+def test_append_validation_errors():
+    import gpumap_gb300 as gm
+
+    p = gm.GPUMAPParams()
+    p.n_instances, p.n_features = 10, 4
+    core = gm._core.GPUMAP(p)
+    with pytest.raises(RuntimeError, match="2D"):
+        core.append_data(np.zeros(4, np.float32))
+    with pytest.raises(RuntimeError, match="float32"):
+        core.append_data(np.zeros((2, 4), np.float64))
+    with pytest.raises(RuntimeError, match="C-contiguous"):
+        core.append_data(np.zeros((4, 8), np.float32)[:, ::2])
+    with pytest.raises(RuntimeError, match="n_features"):
+        core.append_data(np.zeros((2, 5), np.float32))
+    core.append_data(np.zeros((10, 4), np.float32))
+    with pytest.raises(RuntimeError, match="Exceeding"):
+        core.append_data(np.zeros((1, 4), np.float32))
+    from gpumap_gb300.data_loader import ArrayDataLoader
+
+    p2 = gm.GPUMAPParams()
+    p2.min_dist = 1.5
+    with pytest.raises(ValueError, match="min_dist"):
+        gm.GPUMAP(ArrayDataLoader(np.zeros((3, 4), np.float32)), p2)
+    cai = core.get_neighbor_indices().__cuda_array_interface__
+    assert cai["shape"] == (10, 16) and cai["typestr"] == "<u4" and cai["data"][1] is True

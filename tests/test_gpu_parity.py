@@ -1,0 +1,193 @@
+"""GPU engine vs CPU oracle through the C ABI.
+
+Integer/index state (working and published k-NN lists, flags, Bloom bits,
+queues, fuzzy-union COO, trimmed schedule) and every float that feeds a
+comparison (distances, norms, sigma/rho, weights, epochs_per_sample) must be
+bit-identical.  The SGD embedding is Hogwild-parallel on the GPU and sequential
+in the oracle, so it is compared statistically: trustworthiness within 0.01.
+"""
+import numpy as np
+import pytest
+
+from gpumap_gb300.datasets import gaussian_mixture
+from oracle.knn import exact_knn, recall_at_k, trustworthiness
+
+pytestmark = pytest.mark.gpu
+
+F32, I32, U32 = np.float32, np.int32, np.uint32
+STATE = [("norms", F32), ("x", F32), ("graph_ids", I32), ("graph_dists", F32), ("knn_ids", I32),
+         ("knn_dists", F32), ("pub_idx", U32), ("pub_dist", F32), ("bloom", U32)]
+EMBED = [("sigma", F32), ("rho", F32), ("coo_row", I32), ("coo_col", I32), ("coo_val", F32),
+         ("sched_row", I32), ("sched_col", I32), ("sched_eps", F32)]
+
+
+def pair(native, oracle_mod, n, d, k=15, metric=0, max_epoch=40, neg=5):
+    s = native.Session(native.default_params(n_instances=n, n_features=d, n_neighbors=k, metric=metric,
+                                             max_epoch=max_epoch, negative_sample_rate=neg, device=0))
+    o = oracle_mod.OracleSession(n, d, k=k, metric=metric, max_epoch=max_epoch, negative_sample_rate=neg)
+    return s, o
+
+
+def same_result(r, ro):
+    for f in ("n_insertion_ops", "n_update_ops", "n_embedding_ops", "n_inserted_instances",
+              "n_update_changed_edges", "insertion_queue_size", "update_queue_size", "embedding_queue_size",
+              "insertion_completed", "update_completed", "embedding_completed"):
+        assert int(getattr(r, f)) == int(ro[f]), (f, getattr(r, f), ro[f])
+
+
+def same_state(s, o, embed=False, tag=""):
+    for name, dt in STATE + (EMBED if embed else []):
+        a, b = s.copy(name, dt), o.copy(name, dt)
+        assert a.shape == b.shape, (tag, name, a.shape, b.shape)
+        if not np.array_equal(a, b):
+            bad = np.flatnonzero(a != b)
+            raise AssertionError(f"{tag}: {name} differs in {bad.size} of {a.size} entries, first at {bad[:5]}: "
+                                 f"gpu {a[bad[:5]]} oracle {b[bad[:5]]}")
+    assert np.array_equal(s.update_queue(), o.update_queue()), tag
+    sc, so = s.scalars(), o.scalars()
+    assert sc[:10] == so[:10], (tag, sc, so)
+    assert sc[10] == 0, "device error bits set"
+
+
+def test_single_cycle_phases_bitexact(native, oracle_mod):
+    n, d = 1200, 20
+    X, _ = gaussian_mixture(n, d, seed=11)
+    s, o = pair(native, oracle_mod, n, d)
+    s.append_host(X)
+    o.append(X)
+    same_result(s.run(n, 0, 0), o.run(n, 0, 0))
+    same_state(s, o, tag="insertion")
+    same_result(s.run(0, 2 * n, 0), o.run(0, 2 * n, 0))
+    same_state(s, o, tag="update")
+    same_result(s.run(0, 0, n), o.run(0, 0, n))
+    same_state(s, o, embed=True, tag="embedding")
+
+
+@pytest.mark.parametrize("k,metric,d", [(15, 0, 30), (15, 1, 24), (32, 0, 12), (5, 0, 7), (10, 0, 1)])
+def test_progressive_bitexact(native, oracle_mod, k, metric, d):
+    n = 1600
+    X, _ = gaussian_mixture(n, d, seed=k + d)
+    s, o = pair(native, oracle_mod, n, d, k=k, metric=metric, max_epoch=25)
+    for c in range(4):
+        chunk = X[c * 400 : (c + 1) * 400]
+        s.append_host(chunk)
+        o.append(chunk)
+        same_result(s.run(400, 900, 500), o.run(400, 900, 500))
+        same_state(s, o, embed=True, tag=f"cycle {c}")
+    for c in range(2):
+        same_result(s.run(0, 2500, 700), o.run(0, 2500, 700))
+        same_state(s, o, embed=True, tag=f"update-only {c}")
+
+
+def test_c1_config_recall_and_trustworthiness(native, oracle_mod):
+    # 10,000 x 64 mixture, k=15, one run_with_n_ops(10000, 20000, 50000), 200 epochs
+    n, d = 10_000, 64
+    X, _ = gaussian_mixture(n, d, seed=0)
+    s, o = pair(native, oracle_mod, n, d, max_epoch=200)
+    s.append_host(X)
+    o.append(X)
+    same_result(s.run(10_000, 20_000, 50_000), o.run(10_000, 20_000, 50_000))
+    same_state(s, o, embed=True, tag="C1")
+    q = np.arange(0, n, 5)
+    ei, _ = exact_knn(X, 15, queries=q)
+    idx = s.copy("pub_idx", U32).reshape(n, 16)[:, :15]
+    rec = recall_at_k(idx[q], ei)
+    rec_o = recall_at_k(o.neighbor_indices(n)[q], ei)
+    assert rec == rec_o and rec > 0.9, (rec, rec_o)
+    emb = s.copy("embedding", F32).reshape(n, 2)
+    assert np.all(np.isfinite(emb))
+    sample = np.arange(0, n, 10)
+    tw = trustworthiness(X, emb, 15, sample=sample)
+    tw_o = trustworthiness(X, o.embedding(n), 15, sample=sample)
+    assert abs(tw - tw_o) <= 0.01, (tw, tw_o)
+
+
+def test_fuzzy_schedule_operator(native, oracle_mod):
+    import ctypes as C
+
+    import torch
+
+    n, d, k = 900, 9, 15
+    X, _ = gaussian_mixture(n, d, seed=21)
+    o = oracle_mod.OracleSession(n, d, k=k)
+    o.append(X)
+    o.run(n, 2 * n, 0)
+    pidx = o.copy("pub_idx", U32).reshape(n, k + 1)
+    pdst = o.copy("pub_dist", F32).reshape(n, k + 1)
+    # a few unpublished-looking rows exercise the sentinel paths
+    pidx[5, 3:] = 0xFFFFFFFF
+    pdst[5, 3:] = np.finfo(np.float32).max
+    batch = np.random.default_rng(0).choice(n, 333, replace=False).astype(np.int32)
+    ref = oracle_mod.fuzzy_schedule(pidx, pdst, k, True, batch, n_epochs=150, alpha=0.7)
+    dev = torch.device("cuda:0")
+    t_idx = torch.from_numpy(pidx.view(np.int32)).to(dev)
+    t_dst = torch.from_numpy(pdst).to(dev)
+    t_b = torch.from_numpy(batch).to(dev)
+    cap = 2 * len(batch) * k
+    cr, cc, tr, tc = (torch.zeros(cap, dtype=torch.int32, device=dev) for _ in range(4))
+    cv, te = torch.zeros(cap, device=dev), torch.zeros(cap, device=dev)
+    sg, rh = torch.zeros(n, device=dev), torch.zeros(n, device=dev)
+    counts = (C.c_int64 * 4)()
+    scal = (C.c_float * 3)()
+    lib = native.load()
+    native.check(lib.gm_op_fuzzy_schedule(
+        t_idx.data_ptr(), t_dst.data_ptr(), n, k, 1, t_b.data_ptr(), len(batch), 150, 0.7,
+        cr.data_ptr(), cc.data_ptr(), cv.data_ptr(), tr.data_ptr(), tc.data_ptr(), te.data_ptr(),
+        sg.data_ptr(), rh.data_ptr(), counts, scal, C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    nnz, nnz2 = counts[0], counts[2]
+    assert (nnz, counts[1], nnz2, counts[3]) == (ref["nnz"], ref["extras"], ref["nnz2"], ref["max_deg"])
+    assert (scal[0], scal[1], scal[2]) == (np.float32(ref["mean"]), np.float32(ref["max_w"]),
+                                           np.float32(ref["rounding"]))
+    for t, key in ((cr, "coo_row"), (cc, "coo_col"), (cv, "coo_val")):
+        assert np.array_equal(t[:nnz].cpu().numpy(), ref[key]), key
+    for t, key in ((tr, "t_row"), (tc, "t_col"), (te, "t_eps")):
+        assert np.array_equal(t[:nnz2].cpu().numpy(), ref[key]), key
+    assert np.array_equal(sg.cpu().numpy(), ref["sigma"]) and np.array_equal(rh.cpu().numpy(), ref["rho"])
+
+
+def test_sgd_operator_deterministic_case(native, oracle_mod):
+    # disjoint edges and no negative samples: the parallel epoch has no races
+    import ctypes as C
+
+    import torch
+
+    rng = np.random.default_rng(3)
+    n = 1024
+    emb = rng.normal(size=(n, 2)).astype(np.float32)
+    head = np.arange(0, 512, dtype=np.int32)
+    tail = head + 512
+    eps = rng.uniform(1.0, 6.0, size=512).astype(np.float32)
+    ref = oracle_mod.sgd(emb, head, tail, eps, rounding=4.0, alpha0=1.0, a=1.58, b=0.9, n_epochs=60,
+                         negative_sample_rate=0)
+    dev = torch.device("cuda:0")
+    te = torch.from_numpy(emb.copy()).to(dev)
+    th, tt, tp = (torch.from_numpy(a).to(dev) for a in (head, tail, eps))
+    native.check(native.load().gm_op_sgd(te.data_ptr(), n, th.data_ptr(), tt.data_ptr(), tp.data_ptr(), 512,
+                                         4.0, 1.0, 1.0, 1.58, 0.9, 60, 0, 42,
+                                         C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    assert np.array_equal(te.cpu().numpy(), ref)
+
+
+def test_errors_and_edge_cases(native):
+    p = native.default_params(n_instances=8, n_features=3, device=0)
+    s = native.Session(p)
+    s.append_host(np.zeros((0, 3), np.float32))  # empty append is a no-op
+    with pytest.raises(native.GMError) as e:
+        s.append_host(np.zeros((2, 4), np.float32))
+    assert e.value.code == native.GM_ERR_RUNTIME
+    s.append_host(np.ones((1, 3), np.float32))
+    r = s.run(5, 5, 5)
+    assert r.n_insertion_ops == 1 and r.n_inserted_instances == 1
+    s.append_host(np.random.default_rng(0).normal(size=(7, 3)).astype(np.float32))
+    with pytest.raises(native.GMError) as e:
+        s.append_host(np.ones((1, 3), np.float32))
+    assert e.value.code == native.GM_ERR_CAPACITY
+    r = s.run(10, 100, 100)
+    assert r.n_inserted_instances == 8 and r.insertion_completed
+    idx = s.copy("pub_idx", U32).reshape(8, 16)[:, :15]
+    assert np.all((idx < 8) | (idx == 0xFFFFFFFF))
+    assert np.all(np.isfinite(s.copy("embedding", F32)))
+    s.close()
+    with pytest.raises(native.GMError) as e:
+        s.run(1, 1, 1)
+    assert e.value.code == native.GM_ERR_CLOSED

@@ -1,0 +1,194 @@
+"""CPU tests of the oracle's restatement of the reference path: numeric
+pins, NN-Descent quality against the FP64 brute force, the reference quirks
+it reproduces, and fuzzy-set / scheduling invariants."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from gpumap_gb300.datasets import gaussian_mixture
+from oracle.knn import exact_knn, recall_at_k, trustworthiness
+
+FLT_MAX = np.finfo(np.float32).max
+
+
+def _ulps(a, b):
+    a = np.asarray(a, np.float32)
+    b = np.asarray(b, np.float32)
+    ia = a.view(np.int32).astype(np.int64)
+    ib = b.view(np.int32).astype(np.int64)
+    return np.abs(ia - ib)
+
+
+def test_exp_log_pow_accuracy(oracle_mod):
+    lib = oracle_mod.load()
+    xs = np.concatenate([np.linspace(-87.0, 88.0, 4001), np.linspace(-2, 2, 2001)]).astype(np.float32)
+    got = np.array([lib.gmo_expf(float(x)) for x in xs], np.float32)
+    ref = np.exp(xs.astype(np.float64)).astype(np.float32)
+    assert _ulps(got, ref).max() <= 3
+    ys = np.exp(np.linspace(-30, 30, 3001)).astype(np.float32)
+    gl = np.array([lib.gmo_logf(float(y)) for y in ys], np.float32)
+    rl = np.log(ys.astype(np.float64))
+    assert np.max(np.abs(gl - rl)) <= 2e-6 * np.maximum(1.0, np.abs(rl)).max()
+    gp = np.array([lib.gmo_powf(float(y), 0.9) for y in ys[::10]], np.float64)
+    rp = ys[::10].astype(np.float64) ** 0.9
+    assert np.max(np.abs(gp - rp) / rp) < 5e-6
+    assert lib.gmo_expf(-100.0) == 0.0 and lib.gmo_powf(2.0, 0.0) == 1.0
+
+
+def test_philox_uniformity(oracle_mod):
+    lib = oracle_mod.load()
+    words = []
+    for i in range(4096):
+        c = (C.c_uint32 * 4)(i, 7, 0x33, 0)
+        lib.gmo_philox(c, 42, 0)
+        words.extend(c)
+    w = np.array(words, np.uint64)
+    counts = np.bincount((w >> 28).astype(np.int64), minlength=16)
+    exp = len(w) / 16
+    chi2 = np.sum((counts - exp) ** 2 / exp)
+    assert chi2 < 45  # 15 dof, p ~ 1e-4
+    # distinct counters give distinct blocks
+    assert len(set(words)) > 0.999 * len(words)
+
+
+def test_bloom_hashes(oracle_mod):
+    lib = oracle_mod.load()
+
+    def h(v, mul, add):
+        v = (v * mul + add) & 0xFFFFFFFF
+        v ^= (v << 13) & 0xFFFFFFFF
+        v ^= v >> 17
+        v ^= (v << 5) & 0xFFFFFFFF
+        return v
+
+    for v in (0, 1, 12345, 2**31 - 1, 4000000000):
+        assert lib.gmo_bloom_hash(0, v) == h(v, 1103515245, 12345)
+        assert lib.gmo_bloom_hash(1, v) == h(v, 1664525, 1013904223)
+
+
+def _session(oracle_mod, n, d, k=15, **kw):
+    return oracle_mod.OracleSession(n, d, k=k, **kw)
+
+
+def test_single_call_recall_and_trust(oracle_mod):
+    X, _ = gaussian_mixture(1500, 16, seed=0)
+    o = _session(oracle_mod, 1500, 16)
+    o.append(X)
+    r = o.run(1500, 3000, 1500)
+    assert r["n_insertion_ops"] == 1500 and r["insertion_completed"] == 1
+    ei, ed = exact_knn(X, 15)
+    rec = recall_at_k(o.neighbor_indices(1500), ei)
+    assert rec > 0.95, rec
+    # published distances are squared L2 of the listed ids
+    idx = o.neighbor_indices(1500).astype(np.int64)
+    dst = o.neighbor_dists(1500)
+    d2 = ((X[:, None, :].astype(np.float64) - X[idx].astype(np.float64)) ** 2).sum(-1)
+    assert np.max(np.abs(dst - d2) / np.maximum(d2, 1e-3)) < 1e-4
+    tw = trustworthiness(X, o.embedding(1500), 15, sample=np.arange(0, 1500, 3))
+    assert tw > 0.9, tw
+
+
+def test_q1_insertion_keeps_random_neighbours(oracle_mod):
+    # k=15 gives at most 225 two-hop candidates < 256, so the forward merge is
+    # a no-op and new rows keep their random lists at FLT_MAX
+    X, _ = gaussian_mixture(400, 8, seed=1)
+    o = _session(oracle_mod, 400, 8)
+    o.append(X)
+    o.run(400, 0, 0)
+    gd = o.copy("graph_dists", np.float32).reshape(400, 32)
+    assert np.all(gd == FLT_MAX)
+    pub = o.copy("pub_idx", np.uint32).reshape(400, 16)
+    assert np.all(pub[:, 15] == 1)  # every row published with a valid neighbour
+
+
+def test_forward_merge_active_when_256_candidates(oracle_mod):
+    # k=32 allows 256 distinct two-hop candidates; new rows then improve
+    X, _ = gaussian_mixture(3000, 8, seed=2)
+    o = _session(oracle_mod, 3000, 8, k=32)
+    o.append(X)
+    o.run(3000, 0, 0)
+    gd = o.copy("graph_dists", np.float32).reshape(3000, 32)
+    assert np.mean(gd[:, 0] < FLT_MAX) > 0.5
+
+
+def test_progressive_cycles_and_queues(oracle_mod):
+    X, _ = gaussian_mixture(2000, 12, seed=4)
+    o = _session(oracle_mod, 2000, 12, max_epoch=30)
+    last = None
+    for c in range(8):
+        o.append(X[c * 250 : (c + 1) * 250])
+        last = o.run(250, 1000, 600)
+        assert last["n_inserted_instances"] == (c + 1) * 250
+        assert last["insertion_queue_size"] == 0
+        q = o.update_queue()
+        assert len(q) == len(set(q.tolist())) == last["update_queue_size"]
+    assert last["insertion_completed"] == 1
+    for _ in range(4):
+        o.run(0, 4000, 0)
+    ei, _ = exact_knn(X, 15)
+    assert recall_at_k(o.neighbor_indices(2000), ei) > 0.95
+
+
+def test_cosine_rows_normalised(oracle_mod):
+    rng = np.random.default_rng(5)
+    X = rng.normal(size=(300, 20)).astype(np.float32) * 3
+    o = _session(oracle_mod, 300, 20, metric=1)
+    o.append(X)
+    o.run(300, 600, 0)
+    assert np.all(o.copy("norms", np.float32)[:300] == 1.0)
+    xs = o.copy("x", np.float32).reshape(300, 20)
+    assert np.allclose(np.linalg.norm(xs, axis=1), 1.0, atol=1e-5)
+    ei, ed = exact_knn(X, 15, metric="cosine")
+    assert recall_at_k(o.neighbor_indices(300), ei) > 0.9
+
+
+def test_fuzzy_schedule_invariants(oracle_mod):
+    X, _ = gaussian_mixture(800, 10, seed=6)
+    o = _session(oracle_mod, 800, 10)
+    o.append(X)
+    o.run(800, 2000, 0)
+    k = 15
+    pub_idx = o.copy("pub_idx", np.uint32).reshape(800, k + 1)
+    pub_dist = o.copy("pub_dist", np.float32).reshape(800, k + 1)
+    batch = np.arange(0, 800, 2, dtype=np.int32)
+    f = oracle_mod.fuzzy_schedule(pub_idx, pub_dist, k, True, batch)
+    nb = len(batch)
+    assert f["nnz"] == nb * k + f["extras"]
+    w = f["coo_val"]
+    assert np.all((w >= 0) & (w <= 1))
+    rows, cols = f["coo_row"], f["coo_col"]
+    # column 0 of the embed-time k-NN is self: weight 1 self loops (reference quirk)
+    self_loops = rows[: nb * k] == cols[: nb * k]
+    assert np.all(w[: nb * k][self_loops] == 1.0) and self_loops.sum() >= nb
+    # extras are reversed copies of directed edges
+    ext = set(zip(rows[nb * k :].tolist(), cols[nb * k :].tolist()))
+    dirs = set(zip(cols[: nb * k].tolist(), rows[: nb * k].tolist()))
+    assert ext <= dirs
+    # trimmed edges keep w >= max_w / n_epochs, eps = max_w / w >= 1
+    assert f["nnz2"] == int(np.sum(w >= np.float32(f["max_w"]) / np.float32(200)))
+    assert np.all(f["t_eps"] >= 1.0)
+    r = f["rounding"]
+    assert r > 0 and np.log2(r) == int(np.log2(r))
+    # the same graph through a session's embedding call gives the same COO
+    o.run(0, 0, 800)  # full sweep: batch = all rows
+    f_all = oracle_mod.fuzzy_schedule(pub_idx, pub_dist, k, True, np.arange(800, dtype=np.int32))
+    assert np.array_equal(o.copy("coo_row", np.int32), f_all["coo_row"])
+    assert np.array_equal(o.copy("coo_val", np.float32), f_all["coo_val"])
+    assert np.array_equal(o.copy("sched_eps", np.float32), f_all["t_eps"])
+
+
+def test_edge_cases(oracle_mod):
+    o = _session(oracle_mod, 5, 3, k=15)
+    o.append(np.zeros((0, 3), np.float32))
+    o.append(np.ones((1, 3), np.float32))
+    r = o.run(1, 10, 10)
+    assert r["n_insertion_ops"] == 1 and r["n_inserted_instances"] == 1
+    o.append(np.arange(12, dtype=np.float32).reshape(4, 3))
+    r = o.run(10, 10, 10)
+    assert r["n_insertion_ops"] == 4 and r["insertion_completed"] == 1
+    with pytest.raises(RuntimeError):
+        o.append(np.ones((1, 3), np.float32))
+    idx = o.neighbor_indices(5)
+    assert np.all((idx < 5) | (idx == 0xFFFFFFFF))
+    assert np.all(np.isfinite(o.embedding(5)))

@@ -188,7 +188,7 @@ def run_value_step(native, X_dev, n, d, upd, emb, final, stats_on):
 class _Cai:
     def __init__(self, ptr, rows, cols, esz, typestr):
         self.__cuda_array_interface__ = {"version": 3, "shape": (rows, cols), "typestr": typestr,
-                                         "strides": (cols * esz, esz), "data": (ptr, True)}
+                                         "strides": (cols * esz, esz), "data": (ptr, False)}
 
 
 def run_e2e_step(X_host, n, d, upd, emb, final):

@@ -208,8 +208,19 @@ int gm_debug_copy(const gm_session *s, int which, void *host, uint64_t bytes) {
   const auto &es = s->impl->embed_scratch();
   const void *src = nullptr;
   switch (which) {
-    case GM_BUF_GRAPH_IDS: src = st.g_ids; break;
-    case GM_BUF_GRAPH_DISTS: src = st.g_dists; break;
+    case GM_BUF_GRAPH_IDS:
+    case GM_BUF_GRAPH_DISTS: {
+      // working lists are stored as packed (dist, id) keys; unpack on the host
+      const uint64_t cnt = bytes / 4;
+      std::vector<unsigned long long> keys(cnt);
+      cudaStreamSynchronize(s->impl->stream());
+      int rc2 = ck(cudaMemcpy(keys.data(), st.g_key, cnt * 8, cudaMemcpyDeviceToHost), "debug copy");
+      if (rc2) return rc2;
+      uint32_t *o = static_cast<uint32_t *>(host);
+      for (uint64_t i = 0; i < cnt; ++i)
+        o[i] = which == GM_BUF_GRAPH_IDS ? (uint32_t)(keys[i] & 0xffffffffu) : (uint32_t)(keys[i] >> 32);
+      return GM_OK;
+    }
     case GM_BUF_KNN_IDS: src = st.knn_ids; break;
     case GM_BUF_KNN_DISTS: src = st.knn_dists; break;
     case GM_BUF_NORMS: src = st.norms; break;

@@ -160,7 +160,7 @@ GM_D float gm_normal(Philox &g) {
 //   dist = max(0, (|a|^2 + |b|^2) - 2*dot)  (reference: insertion_kernel.cuh:400-403)
 GM_D float canon_dist(float na, float nb, float dot) {
   const float v = __fsub_rn(__fadd_rn(na, nb), __fmul_rn(2.0f, dot));
-  return v < 0.0f ? 0.0f : v;
+  return v <= 0.0f ? 0.0f : v;  // also maps -0 to +0 (key order needs +0)
 }
 
 // Lexicographic (dist, id) order used by every neighbour list.
@@ -195,42 +195,67 @@ GM_D void warp_unlock(int *lock) {
   if ((threadIdx.x & 31) == 0) atomicExch(lock, 0);
 }
 
-// Merges m candidates into node t's 32-wide sorted list under t's lock.
-// Semantics per candidate (reference update_kernel.cuh:310-375 and
-// insertion_kernel.cuh:446-482): skip if its id is already in the list;
-// otherwise insert before the first entry it is lexicographically smaller
-// than, dropping the last entry.  Returns the smallest insert position
-// (kListW if nothing was inserted, -1 if the lock wait ran out).
-GM_D int warp_locked_merge(int t, const int *cids, const float *cds, int m,
-                           int *g_ids, float *g_dists, int *locks, unsigned *err) {
+// ---------------------------------------------------------------------------
+// Working-list entries are 64-bit keys: high word = bits of the non-negative
+// float distance, low word = id.  Unsigned key order is the lexicographic
+// (dist, id) order, and an 8-byte load of one slot is never torn.
+// A placeholder is an entry whose distance is FLT_MAX (a random initial
+// neighbour); the empty slot is (FLT_MAX, INT_MAX).
+// ---------------------------------------------------------------------------
+typedef unsigned long long Key;
+constexpr uint32_t kFltMaxBits = 0x7f7fffffu;
+constexpr Key kEmptyKey = ((Key)kFltMaxBits << 32) | (Key)0x7fffffffu;
+
+GM_HD Key make_key(float d, int id) {
+#ifdef __CUDA_ARCH__
+  const uint32_t b = __float_as_uint(d);
+#else
+  uint32_t b;
+  __builtin_memcpy(&b, &d, 4);
+#endif
+  return ((Key)b << 32) | (Key)(uint32_t)id;
+}
+GM_HD int key_id(Key k) { return (int)(uint32_t)(k & 0xffffffffu); }
+GM_D float key_dist(Key k) { return __uint_as_float((uint32_t)(k >> 32)); }
+GM_HD bool key_is_placeholder(Key k) { return (uint32_t)(k >> 32) == kFltMaxBits; }
+
+// Offers m candidate keys to node t's 32-wide sorted list under t's lock.
+// Per candidate: if its id is listed with a finite distance, nothing
+// happens; if its id is listed as a placeholder, the placeholder is removed
+// and the candidate inserted; otherwise the candidate is inserted before the
+// first entry it is smaller than, dropping the last entry.  (The reference,
+// update_kernel.cuh:310-375, skips any listed id; whether a placeholder was
+// evicted before its id is offered then depends on lock order.  Replacing
+// the placeholder makes the final list independent of the order of offers.)
+// Returns the smallest insert position (kListW if nothing changed, -1 if the
+// lock wait ran out).
+GM_D int warp_locked_merge(int t, const Key *cands, int m, Key *g_key, int *locks,
+                           unsigned *err) {
   const int lane = threadIdx.x & 31;
   if (!warp_lock(&locks[t], err)) return -1;
-  const size_t base = (size_t)t * kListW + lane;
-  int myid = __ldcg(&g_ids[base]);
-  float myd = __ldcg(&g_dists[base]);
+  Key *row = g_key + (size_t)t * kListW;
+  Key mine = __ldcg(&row[lane]);
   int minpos = kListW;
   for (int q = 0; q < m; ++q) {
-    const int cid = cids[q];
-    const float cd = cds[q];
-    if (__any_sync(0xffffffffu, myid == cid)) continue;
-    const unsigned msk = __ballot_sync(0xffffffffu, item_less(cd, cid, myd, myid));
+    const Key ck = cands[q];
+    const int cid = key_id(ck);
+    const unsigned match = __ballot_sync(0xffffffffu, key_id(mine) == cid);
+    if (match) {
+      const int at = __ffs(match) - 1;
+      const Key there = __shfl_sync(0xffffffffu, mine, at);
+      if (!key_is_placeholder(there)) continue;
+      const Key nxt = __shfl_down_sync(0xffffffffu, mine, 1);
+      if (lane >= at) mine = (lane == kListW - 1) ? kEmptyKey : nxt;
+    }
+    const unsigned msk = __ballot_sync(0xffffffffu, ck < mine);
     if (msk == 0u) continue;
     const int pos = __ffs(msk) - 1;
-    const int pid = __shfl_up_sync(0xffffffffu, myid, 1);
-    const float pd = __shfl_up_sync(0xffffffffu, myd, 1);
-    if (lane > pos) {
-      myid = pid;
-      myd = pd;
-    } else if (lane == pos) {
-      myid = cid;
-      myd = cd;
-    }
+    const Key prev = __shfl_up_sync(0xffffffffu, mine, 1);
+    if (lane > pos) mine = prev;
+    else if (lane == pos) mine = ck;
     minpos = min(minpos, pos);
   }
-  if (minpos < kListW) {
-    __stcg(&g_ids[base], myid);
-    __stcg(&g_dists[base], myd);
-  }
+  if (minpos < kListW) __stcg(&row[lane], mine);
   warp_unlock(&locks[t]);
   return minpos;
 }

@@ -77,8 +77,7 @@ Session::Session(const gm_params &p) : p_(p) {
   try {
     st_.X = (float *)dalloc(Nm * st_.ld * sizeof(float));
     st_.norms = (float *)dalloc(Nm * sizeof(float));
-    st_.g_ids = (int *)dalloc(Nm * kListW * sizeof(int));
-    st_.g_dists = (float *)dalloc(Nm * kListW * sizeof(float));
+    st_.g_key = (unsigned long long *)dalloc(Nm * kListW * sizeof(unsigned long long));
     st_.locks = (int *)dalloc(Nm * sizeof(int));
     st_.dirty = (int *)dalloc(Nm * sizeof(int));
     st_.knn_ids = (int *)dalloc(Nm * k * sizeof(int));
@@ -135,11 +134,9 @@ Session::Session(const gm_params &p) : p_(p) {
   // Initial contents: zero features (padding must stay zero), empty lists,
   // "no neighbour" published rows, zero embedding.
   cudaStream_t s = stream_;
-  const uint32_t kFltMaxBits = 0x7f7fffffu;  // FLT_MAX
   ck(cudaMemsetAsync(st_.X, 0, Nm * st_.ld * sizeof(float), s), "memset");
   ck(cudaMemsetAsync(st_.norms, 0, Nm * sizeof(float), s), "memset");
-  fill_u32(st_.g_ids, (uint32_t)kIdSentinel, Nm * kListW, s);
-  fill_u32(st_.g_dists, kFltMaxBits, Nm * kListW, s);
+  fill_u64(st_.g_key, kEmptyKey, Nm * kListW, s);
   ck(cudaMemsetAsync(st_.locks, 0, Nm * sizeof(int), s), "memset");
   ck(cudaMemsetAsync(st_.dirty, 0, Nm * sizeof(int), s), "memset");
   fill_u32(st_.knn_ids, (uint32_t)kIdSentinel, Nm * k, s);

@@ -17,8 +17,7 @@ struct DevState {
   int cosine = 0;
   float *X = nullptr;         // n_cap x ld, zero padded
   float *norms = nullptr;     // n_cap squared L2 norms
-  int *g_ids = nullptr;       // n_cap x 32 working list ids (INT_MAX = empty)
-  float *g_dists = nullptr;   // n_cap x 32 working list squared distances
+  unsigned long long *g_key = nullptr;  // n_cap x 32 working lists, (dist bits << 32 | id)
   int *locks = nullptr;       // n_cap per-node locks (0 = free)
   int *dirty = nullptr;       // n_cap device dirty flags (0/1/2)
   int *knn_ids = nullptr;     // n_cap x k authoritative list, old flag = sign
@@ -52,8 +51,9 @@ struct UpdScratch {
 // Count of kernels launched by this library (all sessions and operators).
 void note_launch(int n = 1);
 uint64_t launch_counter();
-// Fills n 32-bit words at p with v.
+// Fills n 32-bit (64-bit) words at p with v.
 void fill_u32(void *p, uint32_t v, size_t n, cudaStream_t s);
+void fill_u64(void *p, unsigned long long v, size_t n, cudaStream_t s);
 void launch_counter_reset();
 // Exclusive scan of in[0..n) into out[0..n]; out[n] = total.  tmp needs
 // scan_tmp_ints(n) ints.

@@ -38,18 +38,14 @@ __device__ __forceinline__ bool contains(const int *a, int m, int v) {
 // Random unique initial neighbours: up to 16 from the recent window
 // [window_start, n), the rest from [0, n); distances FLT_MAX
 // (reference: initialize_random_neighbors_kernel, insertion_kernel.cuh:170-248).
-__global__ void k_random_init(int *g_ids, float *g_dists, int row0, int nrows,
-                              int n, int window_start, uint64_t seed) {
+__global__ void k_random_init(Key *g_key, int row0, int nrows, int n, int window_start,
+                              uint64_t seed) {
   const int rl = blockIdx.x * blockDim.x + threadIdx.x;
   if (rl >= nrows) return;
   const int gid = row0 + rl;
-  int *ids = g_ids + (size_t)gid * kListW;
-  float *ds = g_dists + (size_t)gid * kListW;
+  Key *row = g_key + (size_t)gid * kListW;
   if (n <= 1) {
-    for (int i = 0; i < kListW; ++i) {
-      ids[i] = kIdSentinel;
-      ds[i] = FLT_MAX;
-    }
+    for (int i = 0; i < kListW; ++i) row[i] = kEmptyKey;
     return;
   }
   Philox g;
@@ -77,14 +73,8 @@ __global__ void k_random_init(int *g_ids, float *g_dists, int row0, int nrows,
     if (c == gid || contains(filled, f, c)) continue;
     filled[f++] = c;
   }
-  for (int i = 0; i < f; ++i) {
-    ids[i] = filled[i];
-    ds[i] = FLT_MAX;
-  }
-  for (int i = f; i < kListW; ++i) {
-    ids[i] = kIdSentinel;
-    ds[i] = FLT_MAX;
-  }
+  for (int i = 0; i < f; ++i) row[i] = make_key(FLT_MAX, filled[i]);
+  for (int i = f; i < kListW; ++i) row[i] = kEmptyKey;
 }
 
 // Two-hop candidates, one warp per batch row.  Position p = kk*k + j visits
@@ -93,7 +83,7 @@ __global__ void k_random_init(int *g_ids, float *g_dists, int row0, int nrows,
 // first 256 kept positions in order are the candidates
 // (reference: sample_forward_candidates_kernel, insertion_kernel.cuh:250-321).
 constexpr int kSampWarps = 4;
-__global__ void k_sample_candidates(const int *g_ids, int row0, int nrows, int n,
+__global__ void k_sample_candidates(const Key *g_key, int row0, int nrows, int n,
                                     int k, int *cand, int *cand_cnt) {
   extern __shared__ int smem_sc[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -104,7 +94,7 @@ __global__ void k_sample_candidates(const int *g_ids, int row0, int nrows, int n
   int *nb = cv + P;
   const int gid = row0 + rl;
   if (lane < k) {
-    const int e = g_ids[(size_t)gid * kListW + lane];
+    const int e = key_id(g_key[(size_t)gid * kListW + lane]);
     nb[lane] = (e >= 0 && e < n) ? e : kIdSentinel;
   }
   __syncwarp();
@@ -113,7 +103,7 @@ __global__ void k_sample_candidates(const int *g_ids, int row0, int nrows, int n
     const int nbr = nb[j];
     int c = -1;
     if (nbr != kIdSentinel) {
-      const int e = g_ids[(size_t)nbr * kListW + kk];
+      const int e = key_id(g_key[(size_t)nbr * kListW + kk]);
       if ((uint32_t)e < (uint32_t)n && e != gid) {
         bool isnb = false;
         for (int q = 0; q < k; ++q) isnb |= (nb[q] == e);
@@ -204,7 +194,7 @@ __global__ void __launch_bounds__(256) k_candidate_dists(
 // reference sorts all 256 slots with -1 sentinels first and stops at the
 // first sentinel (insertion_kernel.cuh:407-534), so the merge only takes
 // effect when all 256 slots hold valid candidates; that rule is kept.
-__global__ void k_forward_merge(int *g_ids, float *g_dists, int row0, int nrows,
+__global__ void k_forward_merge(Key *g_key, int row0, int nrows,
                                 const int *cand, const int *cand_cnt,
                                 const float *cand_dist) {
   const int rl = blockIdx.x * blockDim.x + threadIdx.x;
@@ -239,11 +229,10 @@ __global__ void k_forward_merge(int *g_ids, float *g_dists, int row0, int nrows,
   }
   int lid[kListW];
   float ldv[kListW];
-  int *gl = g_ids + (size_t)gid * kListW;
-  float *gd = g_dists + (size_t)gid * kListW;
+  Key *gk = g_key + (size_t)gid * kListW;
   for (int i = 0; i < kListW; ++i) {
-    lid[i] = gl[i];
-    ldv[i] = gd[i];
+    lid[i] = key_id(gk[i]);
+    ldv[i] = key_dist(gk[i]);
   }
   bool updated = false;
   for (int i = 0; i < kListW; ++i) {
@@ -265,10 +254,7 @@ __global__ void k_forward_merge(int *g_ids, float *g_dists, int row0, int nrows,
     updated = true;
   }
   if (updated)
-    for (int i = 0; i < kListW; ++i) {
-      gl[i] = lid[i];
-      gd[i] = ldv[i];
-    }
+    for (int i = 0; i < kListW; ++i) gk[i] = make_key(ldv[i], lid[i]);
 }
 
 // Reverse step: each (batch row i, existing candidate j, dist) is offered to
@@ -278,12 +264,10 @@ __global__ void k_forward_merge(int *g_ids, float *g_dists, int row0, int nrows,
 // Offers that cannot change j's list (dist above j's last entry, or i
 // already listed) are dropped without taking the lock.
 constexpr int kRevWarps = 8;
-__global__ void k_reverse_insert(int *g_ids, float *g_dists, int *locks, int *dirty,
-                                 unsigned *err, int row0, int nrows,
-                                 const int *cand, const int *cand_cnt,
+__global__ void k_reverse_insert(Key *g_key, int *locks, int *dirty, unsigned *err, int row0,
+                                 int nrows, const int *cand, const int *cand_cnt,
                                  const float *cand_dist) {
-  __shared__ int s_id[kRevWarps];
-  __shared__ float s_d[kRevWarps];
+  __shared__ Key s_key[kRevWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int rl = blockIdx.x * kRevWarps + warp;
   if (rl >= nrows) return;
@@ -292,21 +276,18 @@ __global__ void k_reverse_insert(int *g_ids, float *g_dists, int *locks, int *di
   for (int s0 = 0; s0 < cnt; s0 += 32) {
     const int s = s0 + lane;
     int j = -1;
-    float dv = -1.0f;
+    Key ck = 0;
     bool want = false;
     if (s < cnt) {
       j = cand[(size_t)rl * kMaxCand + s];
-      dv = cand_dist[(size_t)rl * kMaxCand + s];
+      const float dv = cand_dist[(size_t)rl * kMaxCand + s];
       if (j >= 0 && j < row0 && dv >= 0.0f) {
-        const float worst = __ldcg(&g_dists[(size_t)j * kListW + kListW - 1]);
-        if (!(dv > worst)) {
+        ck = make_key(dv, gid);
+        const Key *row = g_key + (size_t)j * kListW;
+        if (ck < __ldcg(&row[kListW - 1])) {
           want = true;
-          const int4 *row = reinterpret_cast<const int4 *>(g_ids + (size_t)j * kListW);
-#pragma unroll
-          for (int w = 0; w < kListW / 4; ++w) {
-            const int4 v = __ldcg(row + w);
-            if (v.x == gid || v.y == gid || v.z == gid || v.w == gid) want = false;
-          }
+          for (int w = 0; w < kListW; ++w)
+            if (__ldcg(&row[w]) == ck) want = false;
         }
       }
     }
@@ -315,14 +296,10 @@ __global__ void k_reverse_insert(int *g_ids, float *g_dists, int *locks, int *di
       const int src = __ffs(bal) - 1;
       bal &= bal - 1u;
       const int tj = __shfl_sync(0xffffffffu, j, src);
-      const float td = __shfl_sync(0xffffffffu, dv, src);
-      if (lane == 0) {
-        s_id[warp] = gid;
-        s_d[warp] = td;
-      }
+      const Key tk = __shfl_sync(0xffffffffu, ck, src);
+      if (lane == 0) s_key[warp] = tk;
       __syncwarp();
-      const int pos = warp_locked_merge(tj, &s_id[warp], &s_d[warp], 1, g_ids,
-                                        g_dists, locks, err);
+      const int pos = warp_locked_merge(tj, &s_key[warp], 1, g_key, locks, err);
       if (lane == 0 && pos >= 0 && pos < kListW) dirty[tj] = 1;
       __syncwarp();
     }
@@ -333,8 +310,7 @@ __global__ void k_reverse_insert(int *g_ids, float *g_dists, int *locks, int *di
 // reference's CPU diff, insertion_kernel.cuh:1034-1089) and publishes the row
 // with sentinels for invalid or self ids plus the validity flag in column k
 // (impl.cuh:103-144, matrix_utils.cuh:128-174).
-__global__ void k_adopt_publish(const int *g_ids, const float *g_dists,
-                                int *knn_ids, float *knn_dists, uint32_t *pub_idx,
+__global__ void k_adopt_publish(const Key *g_key, int *knn_ids, float *knn_dists, uint32_t *pub_idx,
                                 float *pub_dist, int k, int row0, int nrows,
                                 const int *rows, const int *n_rows_dev, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -343,8 +319,9 @@ __global__ void k_adopt_publish(const int *g_ids, const float *g_dists,
   const int row = (i < nrows) ? row0 + i : rows[i - nrows];
   bool valid_row = false;
   for (int j = 0; j < k; ++j) {
-    const int e = g_ids[(size_t)row * kListW + j];
-    const float dv = g_dists[(size_t)row * kListW + j];
+    const Key key = g_key[(size_t)row * kListW + j];
+    const int e = key_id(key);
+    const float dv = key_dist(key);
     knn_ids[(size_t)row * k + j] = e;
     knn_dists[(size_t)row * k + j] = dv;
     const int id = e >= 0 ? e : -e - 1;
@@ -359,7 +336,7 @@ __global__ void k_adopt_publish(const int *g_ids, const float *g_dists,
 // New rows' embedding: N(0,1), then (if a pre-batch neighbour has a finite
 // distance) the exp(-(d - d_min))-weighted mean of the pre-batch neighbours
 // (reference: insertion_kernel.cuh:790-907).
-__global__ void k_embed_init(const int *g_ids, const float *g_dists, float *emb,
+__global__ void k_embed_init(const Key *g_key, float *emb,
                              int k, int row0, int nrows, int n) {
   const int rl = blockIdx.x * blockDim.x + threadIdx.x;
   if (rl >= nrows) return;
@@ -368,10 +345,13 @@ __global__ void k_embed_init(const int *g_ids, const float *g_dists, float *emb,
   philox_init(g, 42ull, (uint32_t)row, kTagInitEmbedding);
   float e0 = gm_normal(g);
   float e1 = gm_normal(g);
-  const int *ids = g_ids + (size_t)row * kListW;
-  const float *ds = g_dists + (size_t)row * kListW;
+  const Key *keys = g_key + (size_t)row * kListW;
+  int ids[kListW];
+  float ds[kListW];
   float dmin = FLT_MAX;
   for (int j = 0; j < k; ++j) {
+    ids[j] = key_id(keys[j]);
+    ds[j] = key_dist(keys[j]);
     const int id = ids[j];
     if (id < 0 || id >= n || id >= row0) continue;
     if (ds[j] < dmin) dmin = ds[j];
@@ -409,8 +389,8 @@ void launch_row_norms(const DevState &st, int row0, int nrows, cudaStream_t s) {
 void launch_random_init(const DevState &st, int row0, int nrows, int n,
                         int window_start, uint64_t seed, cudaStream_t s) {
   if (nrows <= 0) return;
-  k_random_init<<<cdiv(nrows, 128), 128, 0, s>>>(st.g_ids, st.g_dists, row0, nrows,
-                                                 n, window_start, seed);
+  k_random_init<<<cdiv(nrows, 128), 128, 0, s>>>(st.g_key, row0, nrows, n, window_start,
+                                                 seed);
   note_launch();
 }
 
@@ -419,7 +399,7 @@ void launch_sample_candidates(const DevState &st, int row0, int nrows, int n,
   if (nrows <= 0) return;
   const size_t smem = (size_t)kSampWarps * (kListW + st.k * st.k) * sizeof(int);
   k_sample_candidates<<<cdiv(nrows, kSampWarps), kSampWarps * 32, smem, s>>>(
-      st.g_ids, row0, nrows, n, st.k, cand, cand_cnt);
+      st.g_key, row0, nrows, n, st.k, cand, cand_cnt);
   note_launch();
 }
 
@@ -436,8 +416,8 @@ void launch_forward_merge(const DevState &st, int row0, int nrows,
                           const int *cand, const int *cand_cnt,
                           const float *cand_dist, cudaStream_t s) {
   if (nrows <= 0) return;
-  k_forward_merge<<<cdiv(nrows, 64), 64, 0, s>>>(st.g_ids, st.g_dists, row0, nrows,
-                                                 cand, cand_cnt, cand_dist);
+  k_forward_merge<<<cdiv(nrows, 64), 64, 0, s>>>(st.g_key, row0, nrows, cand, cand_cnt,
+                                                 cand_dist);
   note_launch();
 }
 
@@ -446,8 +426,7 @@ void launch_reverse_insert(const DevState &st, int row0, int nrows,
                            const float *cand_dist, cudaStream_t s) {
   if (nrows <= 0 || row0 <= 0) return;
   k_reverse_insert<<<cdiv(nrows, kRevWarps), kRevWarps * 32, 0, s>>>(
-      st.g_ids, st.g_dists, st.locks, st.dirty, st.err, row0, nrows, cand, cand_cnt,
-      cand_dist);
+      st.g_key, st.locks, st.dirty, st.err, row0, nrows, cand, cand_cnt, cand_dist);
   note_launch();
 }
 
@@ -457,16 +436,15 @@ void launch_adopt_and_publish(const DevState &st, int row0, int nrows,
   const int total = nrows + n_rows_max;
   if (total <= 0) return;
   k_adopt_publish<<<cdiv(total, 128), 128, 0, s>>>(
-      st.g_ids, st.g_dists, st.knn_ids, st.knn_dists, st.pub_idx, st.pub_dist, st.k,
-      row0, nrows, rows, n_rows_dev, n);
+      st.g_key, st.knn_ids, st.knn_dists, st.pub_idx, st.pub_dist, st.k, row0, nrows,
+      rows, n_rows_dev, n);
   note_launch();
 }
 
 void launch_embed_init(const DevState &st, int row0, int nrows, int n,
                        cudaStream_t s) {
   if (nrows <= 0) return;
-  k_embed_init<<<cdiv(nrows, 128), 128, 0, s>>>(st.g_ids, st.g_dists, st.emb, st.k,
-                                                row0, nrows, n);
+  k_embed_init<<<cdiv(nrows, 128), 128, 0, s>>>(st.g_key, st.emb, st.k, row0, nrows, n);
   note_launch();
 }
 

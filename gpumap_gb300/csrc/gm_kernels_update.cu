@@ -168,17 +168,16 @@ struct LJSmem {
   float As[kLJKC][kLJR + 4];
   float Bs[kLJKC][kLJC + 4];
   float D[kLJR][kLJC + 1];
-  int lst[kLJWarps][kListW];
-  int cb_id[kLJWarps][kLJC];
-  float cb_d[kLJWarps][kLJC];
+  Key lst[kLJWarps][kListW];
+  Key cb[kLJWarps][kLJC];
   int nN, nC;
 };
 
 __global__ void __launch_bounds__(kLJThreads) k_local_join(
     const int *join_nodes, const int *n_join_dev, const int *fwd_new,
     const int *fwd_old, const int *rev_new, const int *rev_old, const int4 *sizes,
-    const float *X, const float *norms, int ld, int d, int n, int k, int *g_ids,
-    float *g_dists, int *locks, int *dirty, unsigned *err, unsigned long long *stat) {
+    const float *X, const float *norms, int ld, int d, int n, int k, Key *g_key,
+    int *locks, int *dirty, unsigned *err, unsigned long long *stat) {
   extern __shared__ __align__(16) unsigned char lj_raw[];
   LJSmem &S = *reinterpret_cast<LJSmem *>(lj_raw);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -293,45 +292,41 @@ __global__ void __launch_bounds__(kLJThreads) k_local_join(
     }
     __syncthreads();
 
-    // ---- offer pairs to both endpoints, one target per warp at a time
+    // ---- offer pairs to both endpoints, one target per warp at a time.
+    // An offer can only act if it is below the target's last entry and not
+    // already listed with this distance; the snapshot (8-byte slots, never
+    // torn) filters the rest without taking the lock.
     for (int tt = warp; tt < nC; tt += kLJWarps) {
       const int idt = S.cid[tt];
-      const size_t lb = (size_t)idt * kListW + lane;
-      const int snap_id = __ldcg(&g_ids[lb]);
-      const float worst = __shfl_sync(0xffffffffu, __ldcg(&g_dists[lb]), kListW - 1);
-      S.lst[warp][lane] = snap_id;
+      S.lst[warp][lane] = __ldcg(&g_key[(size_t)idt * kListW + lane]);
       __syncwarp();
+      const Key worst = S.lst[warp][kListW - 1];
       const int ncand = (tt < nN) ? nC : nN;
       int m = 0;
       for (int c0b = 0; c0b < ncand; c0b += 32) {
         const int c = c0b + lane;
         bool pass = false;
-        int cidv = 0;
-        float dv = 0.0f;
+        Key ck = 0;
         if (c < ncand && c != tt) {
-          cidv = S.cid[c];
-          dv = (tt < nN) ? S.D[tt][c] : S.D[c][tt];
-          if (cidv != idt && !(dv > worst)) {
+          const int cidv = S.cid[c];
+          const float dv = (tt < nN) ? S.D[tt][c] : S.D[c][tt];
+          ck = make_key(dv, cidv);
+          if (cidv != idt && ck < worst) {
             pass = true;
             for (int q = 0; q < kListW; ++q)
-              if (S.lst[warp][q] == cidv) {
+              if (S.lst[warp][q] == ck) {
                 pass = false;
                 break;
               }
           }
         }
         const unsigned bal = __ballot_sync(0xffffffffu, pass);
-        if (pass) {
-          const int idx = m + __popc(bal & ((1u << lane) - 1u));
-          S.cb_id[warp][idx] = cidv;
-          S.cb_d[warp][idx] = dv;
-        }
+        if (pass) S.cb[warp][m + __popc(bal & ((1u << lane) - 1u))] = ck;
         m += __popc(bal);
       }
       __syncwarp();
       if (m > 0) {
-        const int pos = warp_locked_merge(idt, S.cb_id[warp], S.cb_d[warp], m, g_ids,
-                                          g_dists, locks, err);
+        const int pos = warp_locked_merge(idt, S.cb[warp], m, g_key, locks, err);
         if (lane == 0) {
           if (pos >= 0 && pos < kListW) atomicMax(&dirty[idt], pos < k ? 2 : 1);
           if (stat) atomicAdd(&stat[3], 1ull);
@@ -347,7 +342,7 @@ __global__ void __launch_bounds__(kLJThreads) k_local_join(
 // Rows whose working list did not change merge to a no-op, so they are
 // skipped.
 __global__ void k_merge_publish(const int *rows, const int *n_rows_dev,
-                                const int *g_ids, const float *g_dists, int *knn_ids,
+                                const Key *g_key, int *knn_ids,
                                 float *knn_dists, const int *dirty,
                                 uint32_t *pub_idx, float *pub_dist, int k, int n,
                                 int *edge_counter, int *report_flag) {
@@ -364,9 +359,10 @@ __global__ void k_merge_publish(const int *rows, const int *n_rows_dev,
   }
   int h = 0, edges = 0;
   for (int j = 0; j < kListW; ++j) {
-    const float nd = g_dists[(size_t)row * kListW + j];
+    const Key key = g_key[(size_t)row * kListW + j];
+    const float nd = key_dist(key);
     if (nd == FLT_MAX) break;
-    const int nid = g_ids[(size_t)row * kListW + j];
+    const int nid = key_id(key);
     if (nid < 0 || nid >= n || nid == row) continue;
     // insert_to_ordered_list (update_kernel.cuh:87-120)
     if (nd > ldv[k - 1]) continue;
@@ -483,8 +479,7 @@ void launch_local_join(const DevState &st, const UpdScratch &u, const int *join_
   const int grid = std::min(n_join_max, dev < 32 ? ctas[dev] : 1024);
   k_local_join<<<grid, kLJThreads, smem, s>>>(
       join_nodes, n_join_dev, u.fwd_new, u.fwd_old, u.rev_new, u.rev_old, u.sizes, st.X,
-      st.norms, st.ld, st.d, n, st.k, st.g_ids, st.g_dists, st.locks, st.dirty, st.err,
-      st.stat);
+      st.norms, st.ld, st.d, n, st.k, st.g_key, st.locks, st.dirty, st.err, st.stat);
   note_launch();
 }
 
@@ -499,7 +494,7 @@ void launch_merge_publish(const DevState &st, const UpdScratch &u, const int *ro
                           int *edge_counter, int *report_flag, cudaStream_t s) {
   if (n_rows_max <= 0) return;
   k_merge_publish<<<std::min(cdiv(n_rows_max, 128), 2048), 128, 0, s>>>(
-      rows, n_rows_dev, st.g_ids, st.g_dists, st.knn_ids, st.knn_dists, st.dirty,
+      rows, n_rows_dev, st.g_key, st.knn_ids, st.knn_dists, st.dirty,
       st.pub_idx, st.pub_dist, st.k, n, edge_counter, report_flag);
   note_launch();
   (void)u;

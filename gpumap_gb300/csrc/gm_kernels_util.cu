@@ -162,7 +162,19 @@ __global__ void k_fill_u32(uint32_t *p, uint32_t v, size_t n) {
        i += (size_t)gridDim.x * blockDim.x)
     p[i] = v;
 }
+__global__ void k_fill_u64(unsigned long long *p, unsigned long long v, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
 }  // namespace
+
+void fill_u64(void *p, unsigned long long v, size_t n, cudaStream_t s) {
+  if (n == 0) return;
+  const size_t blocks = std::min<size_t>((n + 255) / 256, 4096);
+  k_fill_u64<<<(unsigned)blocks, 256, 0, s>>>((unsigned long long *)p, v, n);
+  note_launch();
+}
 
 void fill_u32(void *p, uint32_t v, size_t n, cudaStream_t s) {
   if (n == 0) return;

@@ -10,6 +10,8 @@ object.
 """
 from __future__ import annotations
 
+import types
+
 import numpy as np
 from scipy.optimize import curve_fit
 
@@ -42,10 +44,14 @@ def _device_array(cai_obj):
         pass
     try:
         import torch
-
-        return torch.as_tensor(cai_obj, device="cuda")
-    except Exception:
+    except ImportError:
         return cai_obj
+    # torch does not take read-only interfaces; hand it a writable-flagged
+    # copy of the same description (the memory is the engine's either way).
+    iface = dict(cai_obj.__cuda_array_interface__)
+    iface["data"] = (iface["data"][0], False)
+    holder = types.SimpleNamespace(__cuda_array_interface__=iface)
+    return torch.as_tensor(holder, device="cuda")
 
 
 class GPUMAP:

@@ -165,10 +165,25 @@ struct Session {
   int last_extra = 0, last_maxdeg = 0;
 };
 
-// ---- working-list insertion (update_kernel.cuh:310-375 semantics) --------
-int list_insert(int *ids, float *ds, int cid, float cd) {
+// ---- working-list offer (update_kernel.cuh:310-375 semantics) ------------
+// An id already listed with a finite distance is skipped (the reference's
+// rule).  An id listed as a placeholder -- a random initial neighbour at
+// FLT_MAX -- is replaced: the placeholder is removed and the offer inserted.
+// The reference skips those too, which makes its result depend on whether
+// the placeholder was evicted before the offer arrived (lock order); the
+// replacement rule gives the same list for any order of offers.
+int list_offer(int *ids, float *ds, int cid, float cd) {
   for (int i = 0; i < W; ++i)
-    if (ids[i] == cid) return W;
+    if (ids[i] == cid) {
+      if (ds[i] != FLT_MAX) return W;
+      for (int q = i; q < W - 1; ++q) {
+        ids[q] = ids[q + 1];
+        ds[q] = ds[q + 1];
+      }
+      ids[W - 1] = SENT;
+      ds[W - 1] = FLT_MAX;
+      break;
+    }
   int pos = W;
   for (int i = 0; i < W; ++i)
     if (less_item(cd, cid, ds[i], ids[i])) {
@@ -190,7 +205,7 @@ float dist_of(const Session &S, size_t a, size_t b) {
   float dot = 0.0f;
   for (size_t i = 0; i < S.d; ++i) dot = fmaf(xa[i], xb[i], dot);
   const float v = (S.norms[a] + S.norms[b]) - 2.0f * dot;
-  return v < 0.0f ? 0.0f : v;
+  return v <= 0.0f ? 0.0f : v;
 }
 
 void publish_row(Session &S, size_t row, size_t n, bool always_flag) {
@@ -383,7 +398,7 @@ uint32_t insert(Session &S, uint32_t n_ops) {
           const int j = cand[rl * MAXC + s];
           const float dv = cdist[rl * MAXC + s];
           if (j < 0 || (size_t)j >= row0 || dv < 0.0f) continue;
-          if (list_insert(&S.gid[(size_t)j * W], &S.gd[(size_t)j * W], (int)(row0 + rl), dv) < W)
+          if (list_offer(&S.gid[(size_t)j * W], &S.gd[(size_t)j * W], (int)(row0 + rl), dv) < W)
             S.dirty[j] = 1;
         }
   }
@@ -507,7 +522,7 @@ size_t update_round(Session &S, std::vector<uint32_t> batch, std::vector<uint32_
     }
     auto offer = [&](int t, int c, float dv) {
       if (t == c) return;
-      const int pos = list_insert(&S.gid[(size_t)t * W], &S.gd[(size_t)t * W], c, dv);
+      const int pos = list_offer(&S.gid[(size_t)t * W], &S.gd[(size_t)t * W], c, dv);
       if (pos < W) S.dirty[t] = std::max(S.dirty[t], pos < k ? 2 : 1);
     };
     for (size_t r = 0; r < N.size(); ++r)
@@ -1057,7 +1072,7 @@ int gmo_copy(gmo_session *o, int which, void *out, uint64_t bytes) {
 uint64_t gmo_size(gmo_session *o, int which) {
   Session &S = o->s;
   switch (which) {
-    case 6: return S.sigma.size() * 4;
+    case 6: case 7: return S.sigma.size() * 4;
     case 8: case 9: case 10: return S.coo_r.size() * 4;
     case 11: case 12: case 13: return S.t_r.size() * 4;
     default: return 0;

@@ -349,13 +349,14 @@ int gm_op_sgd(float *emb, int64_t n, const int32_t *head, const int32_t *tail,
     int iscal[16] = {0};
     float fscal[16] = {0};
     iscal[2] = (int)nnz;
+    iscal[gm::kIscalN] = (int)n;
     fscal[2] = rounding;
     cudaMemcpyAsync(sc, iscal, 64, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync((char *)sc + 64, fscal, 64, cudaMemcpyHostToDevice, s);
     gm::launch_epoch_init(eps, (int)nnz, neg_rate, (float *)ns, (float *)nn, s);
-    gm::launch_sgd(emb, (int)n, head, tail, eps, (float *)ns, (float *)nn, (const int *)sc,
-                   (const float *)((char *)sc + 64), (int)nnz, alpha0, gamma, a, b, n_epochs,
-                   neg_rate, seed, s);
+    gm::launch_sgd(emb, head, tail, eps, (float *)ns, (float *)nn, (const int *)sc,
+                   (const float *)((char *)sc + 64), (int)((nnz + 255) / 256), alpha0, gamma, a,
+                   b, n_epochs, neg_rate, seed, s);
     const cudaError_t err = cudaStreamSynchronize(s);
     cudaFree(ns);
     cudaFree(nn);

@@ -160,6 +160,7 @@ Session::Session(const gm_params &p) : p_(p) {
 
 Session::~Session() {
   if (stream_) cudaStreamSynchronize(stream_);
+  if (sgd_exec_) cudaGraphExecDestroy(sgd_exec_);
   for (auto &e : ev_pool_) cudaEventDestroy(e);
   for (auto &pr : ev_pending_) {
     cudaEventDestroy(pr.a);
@@ -507,10 +508,9 @@ size_t Session::update_round(std::vector<uint32_t> &batch, std::vector<uint32_t>
   timed_begin(0);
   launch_local_join(st_, us_, d_rows_, d_cnt_ + 3, n, n, s);
   timed_end(0);
-  compact_flags(st_.dirty, n, -1, d_rows2_, d_cnt_ + 0, d_tmp_, s);
   ck(cudaMemsetAsync(d_cnt_ + 1, 0, sizeof(int), s), "edges");
-  launch_merge_publish(st_, us_, d_rows2_, d_cnt_ + 0, n, n, d_cnt_ + 1, us_.hflag, s);
-  compact_list(d_rows2_, d_cnt_ + 0, n, us_.hflag, d_rows_, d_cnt_ + 2, d_tmp_, s);
+  launch_merge_publish(st_, us_, nullptr, nullptr, n, n, d_cnt_ + 1, us_.hflag, s);
+  compact_flags(us_.hflag, n, -1, d_rows_, d_cnt_ + 2, d_tmp_, s);
   ck(cudaMemcpyAsync(h_pin_, d_cnt_, 4 * sizeof(int), cudaMemcpyDeviceToHost, s), "counts");
   sync();
   const int edges = (int)h_pin_[1];
@@ -573,9 +573,10 @@ uint32_t Session::embed(uint32_t n_ops) {
   if (sweeps_ > 2) emb_done_ = upd_done_;
   const uint64_t noise_seed = 42ull ^ (uint64_t)sweeps_;
   launch_add_noise(st_.emb, ni, d_batch_, nb, 0.001f, noise_seed, es_, s);
+  launch_schedule(ni, nb, k, p_.alpha, (int)p_.max_epoch, (int)p_.negative_sample_rate, es_, s);
+  launch_set_int(es_.iscal + kIscalN, ni, s);
   timed_begin(2);
-  launch_optimize_layout(st_.emb, ni, nb, k, p_.alpha, 1.0f, p_.a, p_.b, (int)p_.max_epoch,
-                         (int)p_.negative_sample_rate, 42ull, es_, s);
+  run_sgd_graph();
   timed_end(2);
   const int nu = ni - nb;
   if (nu > 0) {
@@ -585,6 +586,37 @@ uint32_t Session::embed(uint32_t n_ops) {
     launch_heuristic(st_.pub_idx, st_.pub_dist, ni, k, euclid, es_.unsel, nu, st_.emb, es_, s);
   }
   return (uint32_t)nb;
+}
+
+// The max_epoch SGD launches of one embedding call, captured once as a CUDA
+// graph and replayed: every parameter is fixed for the session (sizes are read
+// from device scalars), so only a reallocation of the edge buffers forces a
+// new capture.
+void Session::run_sgd_graph() {
+  if (p_.max_epoch == 0) return;
+  if (sgd_grid_ == 0) {
+    int sms = 0;
+    ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_), "attr");
+    sgd_grid_ = 4 * std::max(sms, 1);
+  }
+  bool fresh = false;
+  if (!sgd_exec_ || sgd_key_ != (const void *)es_.t_row) {
+    if (sgd_exec_) cudaGraphExecDestroy(sgd_exec_);
+    sgd_exec_ = nullptr;
+    cudaGraph_t g = nullptr;
+    ck(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture begin");
+    launch_sgd(st_.emb, es_.t_row, es_.flag_tail, es_.t_val, es_.next_s, es_.next_n, es_.iscal,
+               es_.fscal, sgd_grid_, p_.alpha, 1.0f, p_.a, p_.b, (int)p_.max_epoch,
+               (int)p_.negative_sample_rate, 42ull, stream_);
+    ck(cudaStreamEndCapture(stream_, &g), "capture end");
+    const cudaError_t e = cudaGraphInstantiate(&sgd_exec_, g, 0);
+    cudaGraphDestroy(g);
+    ck(e, "graph instantiate");
+    sgd_key_ = (const void *)es_.t_row;
+    fresh = true;
+  }
+  ck(cudaGraphLaunch(sgd_exec_, stream_), "graph launch");
+  if (!fresh) note_launch((int)p_.max_epoch);
 }
 
 void Session::close() {

@@ -88,6 +88,7 @@ class Session {
   void timed_begin(int slot);
   void timed_end(int slot);
   void collect_timings();
+  void run_sgd_graph();
 
   gm_params p_;
   int device_ = 0;
@@ -127,6 +128,11 @@ class Session {
   std::vector<EvPair> ev_pending_;
   std::vector<cudaEvent_t> ev_pool_;
   unsigned long long *d_stat_ = nullptr;
+
+  // captured SGD epochs
+  cudaGraphExec_t sgd_exec_ = nullptr;
+  const void *sgd_key_ = nullptr;
+  int sgd_grid_ = 0;
 };
 
 }  // namespace gm

@@ -155,11 +155,14 @@ void launch_schedule(int n, int nb, int k, float alpha0, int n_epochs, int neg_r
                      EmbedScratch &e, cudaStream_t s);
 void launch_mark_rows(const int *rows, int nr, int *flag, cudaStream_t s);
 // SGD epochs on scheduled edges; next_s/next_n initialised; nnz in
-// iscal[2], rounding factor in fscal[2].
-void launch_sgd(float *emb, int n, const int *head, const int *tail, const float *eps,
+// iscal[2], rows n in iscal[4], rounding factor in fscal[2].  grid blocks of
+// 256 threads stride over the edges, so a fixed grid can be captured once.
+void launch_sgd(float *emb, const int *head, const int *tail, const float *eps,
                 float *next_s, float *next_n, const int *iscal, const float *fscal,
-                int nnz_max, float alpha0, float gamma, float a, float b, int n_epochs,
+                int grid, float alpha0, float gamma, float a, float b, int n_epochs,
                 int neg_rate, uint64_t seed, cudaStream_t s);
+void launch_set_int(int *p, int v, cudaStream_t s);
+constexpr int kIscalN = 4;
 void launch_epoch_init(const float *eps, int nnz, int neg_rate, float *next_s,
                        float *next_n, cudaStream_t s);
 void launch_add_noise(float *emb, int n, const int *batch, int nb,

@@ -9,9 +9,10 @@ namespace gm {
 
 // Scalar slots in EmbedScratch.
 //   fscal: 0 mean_dist, 1 max_w, 2 rounding, 3 x_min, 4 x_max
-//   iscal: 0 nnz (directed + extras), 1 extras, 2 nnz after trim, 3 max degree
+//   iscal: 0 nnz (directed + extras), 1 extras, 2 nnz after trim, 3 max degree,
+//          4 rows n (read by the SGD epochs so a captured graph stays valid)
 enum { FS_MEAN = 0, FS_MAXW = 1, FS_ROUND = 2, FS_XMIN = 3, FS_XMAX = 4 };
-enum { IS_NNZ = 0, IS_EXTRA = 1, IS_NNZ2 = 2, IS_MAXDEG = 3 };
+enum { IS_NNZ = 0, IS_EXTRA = 1, IS_NNZ2 = 2, IS_MAXDEG = 3, IS_N = 4 };
 
 namespace {
 
@@ -260,10 +261,11 @@ GM_D float trunc_grad(float rounding, float x) {
 // One SGD epoch (reference optimize_batch_kernel, :509-589; Hogwild
 // updates, tail moved by rounded atomics, head accumulated then added).
 __global__ void k_sgd_epoch(float *emb, const int *head, const int *tail,
-                            const int *iscal, int n, const float *eps, float *next_s,
+                            const int *iscal, const float *eps, float *next_s,
                             float *next_n, float alpha, int epoch, float gamma, float a,
                             float b, float nsr_inv, uint64_t seed, const float *fscal) {
   const int nnz = iscal[IS_NNZ2];
+  const int n = iscal[IS_N];
   const float rounding = fscal[FS_ROUND];
   const float fe = (float)epoch;
   const float bm1 = __fsub_rn(b, 1.0f);
@@ -322,6 +324,8 @@ __global__ void k_sgd_epoch(float *emb, const int *head, const int *tail,
     atomicAdd(cp + 1, trunc_grad(rounding, g1));
   }
 }
+
+__global__ void k_set_int(int *p, int v) { *p = v; }
 
 __global__ void k_epoch_init(const float *eps, int nnz, float nsr_inv, float *next_s,
                              float *next_n) {
@@ -480,8 +484,14 @@ void launch_optimize_layout(float *emb, int n, int nb, int k, float alpha0, floa
                             EmbedScratch &e, cudaStream_t s) {
   launch_schedule(n, nb, k, alpha0, n_epochs, neg_rate, e, s);
   if (n <= 0 || n_epochs <= 0 || nb <= 0) return;
-  launch_sgd(emb, n, e.t_row, e.flag_tail, e.t_val, e.next_s, e.next_n, e.iscal, e.fscal,
-             2 * nb * k, alpha0, gamma, a, b, n_epochs, neg_rate, seed, s);
+  launch_set_int(e.iscal + IS_N, n, s);
+  launch_sgd(emb, e.t_row, e.flag_tail, e.t_val, e.next_s, e.next_n, e.iscal, e.fscal,
+             cdiv(2 * nb * k, 256), alpha0, gamma, a, b, n_epochs, neg_rate, seed, s);
+}
+
+void launch_set_int(int *p, int v, cudaStream_t s) {
+  k_set_int<<<1, 1, 0, s>>>(p, v);
+  note_launch();
 }
 
 void launch_epoch_init(const float *eps, int nnz, int neg_rate, float *next_s,
@@ -492,18 +502,17 @@ void launch_epoch_init(const float *eps, int nnz, int neg_rate, float *next_s,
   note_launch();
 }
 
-void launch_sgd(float *emb, int n, const int *head, const int *tail, const float *eps,
+void launch_sgd(float *emb, const int *head, const int *tail, const float *eps,
                 float *next_s, float *next_n, const int *iscal, const float *fscal,
-                int nnz_max, float alpha0, float gamma, float a, float b, int n_epochs,
+                int grid, float alpha0, float gamma, float a, float b, int n_epochs,
                 int neg_rate, uint64_t seed, cudaStream_t s) {
-  if (n <= 0 || n_epochs <= 0 || nnz_max <= 0) return;
+  if (n_epochs <= 0 || grid <= 0) return;
   const float nsr_inv = 1.0f / (float)neg_rate;
-  const int grid = cdiv(nnz_max, 256);
   float alpha = alpha0;
   uint64_t cur_seed = seed;
   for (int ep = 0; ep < n_epochs; ++ep) {
-    k_sgd_epoch<<<grid, 256, 0, s>>>(emb, head, tail, iscal, n, eps, next_s, next_n, alpha,
-                                     ep, gamma, a, b, nsr_inv, cur_seed, fscal);
+    k_sgd_epoch<<<grid, 256, 0, s>>>(emb, head, tail, iscal, eps, next_s, next_n, alpha, ep,
+                                     gamma, a, b, nsr_inv, cur_seed, fscal);
     note_launch();
     // alpha and seed for the next epoch (reference embedding_kernel.cuh:790-792)
     alpha = alpha0 * (1.0f - (float)ep / (float)n_epochs);

@@ -337,18 +337,19 @@ __global__ void __launch_bounds__(kLJThreads) k_local_join(
   }
 }
 
-// update_graph + sort_lists + publish for the rows whose working list
-// changed this round (reference: update_kernel.cuh:810-878, 986-1050).
-// Rows whose working list did not change merge to a no-op, so they are
-// skipped.
+// update_graph + sort_lists + publish (reference: update_kernel.cuh:810-878,
+// 986-1050) for every row, as the reference does: a row whose working list
+// did not change this round can still gain an entry, when an id that was a
+// placeholder in its k-list (and so skipped as a duplicate) has since been
+// pushed out of the k-list.  rows == nullptr means rows 0..n-1.
 __global__ void k_merge_publish(const int *rows, const int *n_rows_dev,
                                 const Key *g_key, int *knn_ids,
                                 float *knn_dists, const int *dirty,
                                 uint32_t *pub_idx, float *pub_dist, int k, int n,
                                 int *edge_counter, int *report_flag) {
-  const int nr = *n_rows_dev;
+  const int nr = rows ? *n_rows_dev : n;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nr; i += gridDim.x * blockDim.x) {
-  const int row = rows[i];
+  const int row = rows ? rows[i] : i;
   int lid[kListW];
   float ldv[kListW];
   int *kl = knn_ids + (size_t)row * k;

@@ -34,9 +34,13 @@ def test_run_with_n_ops_views():
     assert torch.isfinite(emb).all()
     i64 = idx.to(torch.int64).cpu().numpy()
     assert np.all((i64 >= 0) & (i64 < 3000))
-    # dists are squared L2 of the listed ids
+    # dists are squared L2 of the listed ids; random initial neighbours not yet
+    # re-scored stay at FLT_MAX, as in the reference
     d2 = ((X[:, None, :].astype(np.float64) - X[i64].astype(np.float64)) ** 2).sum(-1)
-    assert np.max(np.abs(dst.cpu().numpy() - d2) / np.maximum(d2, 1e-3)) < 1e-4
+    dn = dst.cpu().numpy()
+    real = dn < np.finfo(np.float32).max
+    assert real.mean() > 0.9
+    assert np.max(np.abs(dn[real] - d2[real]) / np.maximum(d2[real], 1e-3)) < 1e-4
     m.close()
 
 

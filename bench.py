@@ -181,13 +181,13 @@ def run_value_step(native, X_dev, n, d, upd, emb, max_final, stats_on, q_idx, ex
         s.append_device(base + c * row_bytes, m, d)
         s.run(m, upd, emb)
     v = s.view("indices")
-    table = torch.as_tensor(_Cai(v.ptr, n, K + 1, 4, "<u4"), device="cuda")
+    table = torch.as_tensor(_Cai(v.ptr, n, K + 1, 4, "<i4"), device="cuda")  # ids < 2^31
     q_dev = torch.as_tensor(q_idx, device="cuda")
     rec, rounds = 0.0, 0
     while rounds < max_final:
         s.run(0, n, 0)
         rounds += 1
-        rec = recall(table[q_dev, :K].to(torch.int64).cpu().numpy(), exact)
+        rec = recall(table[q_dev, :K].cpu().numpy(), exact)
         if rec >= RECALL_TARGET:
             break
     end.record()

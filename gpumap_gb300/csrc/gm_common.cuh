@@ -185,14 +185,21 @@ GM_D bool warp_lock(int *lock, unsigned *err) {
     }
     if (!ok) atomicOr(err, kDevErrLock);
   }
+  // acquire: every lane is ordered after lane 0's successful CAS
+  __syncwarp();
   ok = __shfl_sync(0xffffffffu, ok, 0);
   __threadfence();
   return ok != 0;
 }
 
 GM_D void warp_unlock(int *lock) {
-  __threadfence();
-  if ((threadIdx.x & 31) == 0) atomicExch(lock, 0);
+  // release: all lanes' list stores precede lane 0's fence and unlock
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) {
+    __threadfence();
+    atomicExch(lock, 0);
+  }
+  __syncwarp();
 }
 
 // ---------------------------------------------------------------------------

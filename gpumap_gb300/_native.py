@@ -22,7 +22,7 @@ GM_ERR_CLOSED = -7
 GM_BUF = {
     "graph_ids": 0, "graph_dists": 1, "knn_ids": 2, "knn_dists": 3, "norms": 4, "bloom": 5,
     "sigma": 6, "rho": 7, "coo_row": 8, "coo_col": 9, "coo_val": 10, "sched_row": 11,
-    "sched_col": 12, "sched_eps": 13, "x": 14, "pub_idx": 15, "pub_dist": 16, "embedding": 17,
+    "sched_col": 12, "sched_eps": 13, "x": 14, "pub_idx": 15, "pub_dist": 16, "embedding": 17, "exact_d": 18,
 }
 
 
@@ -59,7 +59,8 @@ class gm_stats(C.Structure):
         ("join_nodes", C.c_uint64), ("join_rows", C.c_uint64), ("join_pairs", C.c_uint64),
         ("join_merges", C.c_uint64), ("cand_launches", C.c_uint64), ("cand_ms", C.c_double),
         ("cand_rows", C.c_uint64), ("sgd_launches", C.c_uint64), ("sgd_ms", C.c_double),
-        ("phase_s", C.c_double * 3),
+        ("exact_launches", C.c_uint64), ("exact_ms", C.c_double), ("exact_pairs", C.c_uint64),
+        ("exact_rescored", C.c_uint64), ("phase_s", C.c_double * 3),
     ]
 
 

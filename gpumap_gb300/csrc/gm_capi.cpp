@@ -193,6 +193,7 @@ int gm_debug_buffer_size(const gm_session *s, int which, uint64_t *bytes) {
     case GM_BUF_X: *bytes = N * (uint64_t)st.ld * 4; break;
     case GM_BUF_PUB_IDX: case GM_BUF_PUB_DIST: *bytes = N * (k + 1) * 4; break;
     case GM_BUF_EMBEDDING: *bytes = N * 2 * 4; break;
+    case GM_BUF_EXACT_D: *bytes = s->impl->exact_scratch_bytes(); break;
     default: return fail(GM_ERR_INVALID, "unknown buffer");
   }
   return GM_OK;
@@ -237,6 +238,7 @@ int gm_debug_copy(const gm_session *s, int which, void *host, uint64_t bytes) {
     case GM_BUF_PUB_IDX: src = st.pub_idx; break;
     case GM_BUF_PUB_DIST: src = st.pub_dist; break;
     case GM_BUF_EMBEDDING: src = st.emb; break;
+    case GM_BUF_EXACT_D: src = s->impl->exact_scratch(); break;
     default: return fail(GM_ERR_INVALID, "unknown buffer");
   }
   if (bytes == 0) return GM_OK;

@@ -50,7 +50,8 @@ Session::Session(const gm_params &p) : p_(p) {
   if (p.n_features < 1) throw Error(GM_ERR_INVALID, "n_features must be >= 1");
   if (p.metric != GM_METRIC_EUCLIDEAN && p.metric != GM_METRIC_COSINE)
     throw Error(GM_ERR_INVALID, "unknown metric");
-  if (p.precision != 0) throw Error(GM_ERR_INVALID, "precision must be 0 (FP32)");
+  if (p.precision != 0 && p.precision != 1)
+    throw Error(GM_ERR_INVALID, "precision must be 0 (FP32 NN-Descent) or 1 (exact, BF16 tensor cores)");
   if (p.n_instances > (uint64_t)(1u << 30))
     throw Error(GM_ERR_INVALID, "n_instances exceeds 2^30");
   if (p.n_features > (uint64_t)(1u << 24)) throw Error(GM_ERR_INVALID, "n_features too large");
@@ -123,6 +124,16 @@ Session::Session(const gm_params &p) : p_(p) {
     es_.tmp = d_tmp_;
 
     ck(cudaMallocHost((void **)&h_pin_, (Nm + 64) * sizeof(uint32_t)), "cudaMallocHost");
+    if (p.precision == 1) {
+      // BF16 shadow rows plus a block of distance / candidate scratch sized so
+      // that a block holds at most ~512 MB of each
+      dh_ = exact_dh((int)d);
+      xh_ = dalloc(Nm * (size_t)dh_ * 2);
+      ex_block_ = (int)std::max<size_t>(128, std::min<size_t>(4096, ((size_t)512 << 20) / (Nm * 4)));
+      ex_block_ = ex_block_ / 128 * 128;
+      ex_D_ = (float *)dalloc((size_t)ex_block_ * Nm * sizeof(float));
+      ex_cand_ = (int *)dalloc((size_t)ex_block_ * Nm * sizeof(int));
+    }
   } catch (...) {
     for (void *q : allocs_) cudaFree(q);
     allocs_.clear();
@@ -152,8 +163,21 @@ Session::Session(const gm_params &p) : p_(p) {
   ck(cudaMemsetAsync(es_.rho, 0, Nm * sizeof(float), s), "memset");
   ck(cudaMemsetAsync(es_.iscal, 0, 16 * sizeof(int), s), "memset");
   ck(cudaMemsetAsync(es_.fscal, 0, 16 * sizeof(float), s), "memset");
+  if (xh_) ck(cudaMemsetAsync(xh_, 0, Nm * (size_t)dh_ * 2, s), "memset");
   ck(cudaGetLastError(), "init fill");
   ck(cudaStreamSynchronize(s), "init sync");
+  if (xh_) {
+    if (!make_row_maps(xh_, (int)Nm, dh_, &maps_)) {
+      for (void *q : allocs_) cudaFree(q);
+      allocs_.clear();
+      cudaFreeHost(h_pin_);
+      h_pin_ = nullptr;
+      cudaStreamDestroy(stream_);
+      stream_ = nullptr;
+      throw Error(GM_ERR_CUDA, "cuTensorMapEncodeTiled unavailable or failed");
+    }
+    ck(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device_), "attr");
+  }
   upd_q_.reset(N);
   ensure_embed(1);
 }
@@ -286,6 +310,9 @@ void Session::collect_timings() {
       } else if (pr.slot == 2) {
         stats_.sgd_ms += ms;
         stats_.sgd_launches += 1;
+      } else if (pr.slot == 3) {
+        stats_.exact_ms += ms;
+        stats_.exact_launches += 1;
       }
     }
     ev_pool_.push_back(pr.a);
@@ -313,6 +340,8 @@ void Session::get_stats(gm_stats *out) {
   stats_.join_pairs = h[2];
   stats_.join_merges = h[3];
   stats_.cand_rows = h[4];
+  stats_.exact_pairs = h[5];
+  stats_.exact_rescored = h[6];
   stats_.kernel_launches = launch_counter();
   *out = stats_;
 }
@@ -413,16 +442,31 @@ uint32_t Session::insert(uint32_t n_ops) {
     bloom_clean_ = true;
   }
   ck(cudaMemsetAsync(st_.dirty, 0, (size_t)n * sizeof(int), s), "dirty");
-  ensure_cand(B);
   launch_row_norms(st_, row0, nb, s);
-  launch_random_init(st_, row0, nb, n, window_start, seed, s);
-  for (int it = 0; it < kInsertIters; ++it) {
-    launch_sample_candidates(st_, row0, nb, n, cand_, cand_cnt_, s);
-    timed_begin(1);
-    launch_candidate_dists(st_, row0, nb, cand_, cand_cnt_, cand_dist_, s);
-    timed_end(1);
-    launch_forward_merge(st_, row0, nb, cand_, cand_cnt_, cand_dist_, s);
-    if (row0 > 0) launch_reverse_insert(st_, row0, nb, cand_, cand_cnt_, cand_dist_, s);
+  if (p_.precision == 1) {
+    // exact lists: every batch row against every inserted row on the tensor
+    // cores, re-scored in FP32 where the BF16 bound cannot decide
+    launch_to_bf16(st_, xh_, dh_, row0, nb, s);
+    timed_begin(3);
+    for (int b0 = 0; b0 < nb; b0 += ex_block_) {
+      const int rows = std::min(ex_block_, nb - b0);
+      // columns: the rows inserted so far (rows appended but still queued
+      // have no norms or shadow rows yet)
+      launch_exact_block(st_, maps_, dh_, row0, b0, rows, row0 + nb, ex_D_, (long)(row0 + nb),
+                         ex_cand_, (long)(row0 + nb), sms_, s);
+    }
+    timed_end(3);
+  } else {
+    ensure_cand(B);
+    launch_random_init(st_, row0, nb, n, window_start, seed, s);
+    for (int it = 0; it < kInsertIters; ++it) {
+      launch_sample_candidates(st_, row0, nb, n, cand_, cand_cnt_, s);
+      timed_begin(1);
+      launch_candidate_dists(st_, row0, nb, cand_, cand_cnt_, cand_dist_, s);
+      timed_end(1);
+      launch_forward_merge(st_, row0, nb, cand_, cand_cnt_, cand_dist_, s);
+      if (row0 > 0) launch_reverse_insert(st_, row0, nb, cand_, cand_cnt_, cand_dist_, s);
+    }
   }
   // existing rows whose list changed, ascending
   compact_flags(st_.dirty, row0, -1, d_rows_, d_cnt_, d_tmp_, s);

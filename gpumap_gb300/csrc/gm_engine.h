@@ -6,6 +6,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <algorithm>
 #include <deque>
 #include <random>
 #include <stdexcept>
@@ -74,6 +75,10 @@ class Session {
   void reset_stats();
   void debug_scalars(int64_t *out, int n) const;
   const DedupQueue &update_queue() const { return upd_q_; }
+  const float *exact_scratch() const { return ex_D_; }
+  uint64_t exact_scratch_bytes() const {
+    return ex_D_ ? (uint64_t)ex_block_ * std::max<uint64_t>(p_.n_instances, 1) * 4 : 0;
+  }
 
  private:
   uint32_t insert(uint32_t n_ops);
@@ -128,6 +133,15 @@ class Session {
   std::vector<EvPair> ev_pending_;
   std::vector<cudaEvent_t> ev_pool_;
   unsigned long long *d_stat_ = nullptr;
+
+  // exact insertion (precision 1): BF16 shadow rows, TMA maps, block scratch
+  void *xh_ = nullptr;
+  int dh_ = 0;
+  ExactMaps maps_{};
+  float *ex_D_ = nullptr;
+  int *ex_cand_ = nullptr;
+  int ex_block_ = 0;
+  int sms_ = 0;
 
   // captured SGD epochs
   cudaGraphExec_t sgd_exec_ = nullptr;

@@ -94,6 +94,21 @@ void launch_adopt_and_publish(const DevState &st, int row0, int nrows,
 void launch_embed_init(const DevState &st, int row0, int nrows, int n,
                        cudaStream_t s);
 
+// ---- exact insertion on tensor cores (gm_exact.cu) ----
+// Two TMA descriptors over the BF16 shadow rows (boxes of 128 and 256 rows).
+struct ExactMaps {
+  alignas(64) unsigned char a[128];
+  alignas(64) unsigned char b[128];
+};
+int exact_dh(int d);  // shadow row width: d rounded up to 64
+bool make_row_maps(void *xh, int n_cap, int dh, ExactMaps *out);
+void launch_to_bf16(const DevState &st, void *xh, int dh, int row0, int nrows, cudaStream_t s);
+// Exact lists for batch rows [row0+blk0, row0+blk0+nrows) against rows [0, n),
+// and offers of those rows to rows [0, row0).  D, cand: nrows x ldD scratch.
+void launch_exact_block(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
+                        int nrows, int n, float *D, long ldD, int *cand, long cand_ld, int sms,
+                        cudaStream_t s);
+
 // ---- update (gm_kernels_update.cu) ----
 void launch_sample_graph(const DevState &st, const UpdScratch &u,
                          const int *batch, int nb, int n, cudaStream_t s);

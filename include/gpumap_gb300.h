@@ -51,7 +51,9 @@ typedef struct gm_params {
   int32_t metric;                /* GM_METRIC_* */
   uint64_t n_instances;          /* capacity in rows */
   uint64_t n_features;           /* columns per row */
-  int32_t precision;             /* 0 = FP32 distances (only value accepted) */
+  int32_t precision;             /* 0 = the reference's NN-Descent insertion, FP32 (default);
+                                    1 = exact insertion: BF16 tensor-core distance tiles against
+                                        every inserted row, FP32 re-score of the survivors */
   int32_t device;                /* CUDA device ordinal, -1 = current */
 } gm_params;
 
@@ -90,6 +92,10 @@ typedef struct gm_stats {
   uint64_t cand_rows;         /* candidate feature rows loaded */
   uint64_t sgd_launches;
   double sgd_ms;
+  uint64_t exact_launches;    /* exact-insertion blocks (precision 1) */
+  double exact_ms;
+  uint64_t exact_pairs;       /* batch x column pairs formed on the tensor cores */
+  uint64_t exact_rescored;    /* pairs re-scored in FP32 */
   double phase_s[3];          /* insertion / update / embedding seconds */
 } gm_stats;
 

@@ -34,6 +34,8 @@ extern "C" {
 #define GM_BUF_PUB_IDX 15    /* n_instances x (k+1) uint32 published indices (neighbor_indices) */
 #define GM_BUF_PUB_DIST 16   /* n_instances x (k+1) float published distances (neighbor_dists) */
 #define GM_BUF_EMBEDDING 17  /* n_instances x 2 float embedding */
+#define GM_BUF_EXACT_D 18    /* precision 1: approximate distances of the last insertion block,
+                                block rows x (rows inserted so far), row-major */
 
 /* Size in bytes of internal buffer `which`. */
 int gm_debug_buffer_size(const struct gm_session *s, int which, uint64_t *bytes);

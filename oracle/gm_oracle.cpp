@@ -140,6 +140,7 @@ uint32_t bh1(uint32_t v) { v *= 1664525u; v += 1013904223u; v ^= v << 13; v ^= v
 struct Session {
   size_t N, d, ld;
   int k, metric, neg_rate, max_epoch;
+  int precision = 0;  // 1: exact insertion (brute force under the canonical distance)
   float a, b, alpha;
   std::vector<float> X, norms;
   std::vector<int> gid;      // N x 32 working lists
@@ -272,135 +273,154 @@ uint32_t insert(Session &S, uint32_t n_ops) {
       S.norms[r] = acc;
     }
   }
-  // K3: random initial neighbours (insertion_kernel.cuh:170-248)
-  for (size_t r = row0; r < row0 + B; ++r) {
-    int *ids = &S.gid[r * W];
-    float *ds = &S.gd[r * W];
-    for (int i = 0; i < W; ++i) {
-      ids[i] = SENT;
-      ds[i] = FLT_MAX;
-    }
-    if (n <= 1) continue;
-    Rng g;
-    rng_init(g, seed, (uint32_t)r, TAG_INIT_NB);
-    const int max_fill = std::min(W, n - 1);
-    const int wsize = n - wstart;
-    const int quota = std::min(W / 2, std::max(0, wsize - 1));
-    std::vector<int> f;
-    auto has = [&](int c) { return std::find(f.begin(), f.end(), c) != f.end(); };
-    int att = 0;
-    while ((int)f.size() < quota && att < quota * 16) {
-      ++att;
-      const int c = wstart + (int)(rng_next(g) % (uint32_t)wsize);
-      if (c == (int)r || has(c)) continue;
-      f.push_back(c);
-    }
-    for (uint32_t t = 0; (int)f.size() < max_fill && t < (1u << 20); ++t) {
-      const int c = (int)(rng_next(g) % (uint32_t)n);
-      if (c == (int)r || has(c)) continue;
-      f.push_back(c);
-    }
-    for (int c = 0; (int)f.size() < max_fill && c < n; ++c)
-      if (c != (int)r && !has(c)) f.push_back(c);
-    for (size_t i = 0; i < f.size(); ++i) ids[i] = f[i];
-  }
-  std::vector<int> cand(B * MAXC), ccnt(B);
-  std::vector<float> cdist(B * MAXC);
-  for (int it = 0; it < 10; ++it) {
-    // K4: two-hop candidates (insertion_kernel.cuh:250-321)
-    for (size_t rl = 0; rl < B; ++rl) {
-      const int g = (int)(row0 + rl);
-      int nb[W];
-      for (int j = 0; j < k; ++j) {
-        const int e = S.gid[(size_t)g * W + j];
-        nb[j] = (e >= 0 && e < n) ? e : SENT;
-      }
-      int *out = &cand[rl * MAXC];
-      int cnt = 0;
-      for (int kk = 0; kk < k && cnt < MAXC; ++kk)
-        for (int j = 0; j < k && cnt < MAXC; ++j) {
-          if (nb[j] == SENT) continue;
-          const int c = S.gid[(size_t)nb[j] * W + kk];
-          if ((uint32_t)c >= (uint32_t)n || c == g) continue;
-          bool skip = false;
-          for (int q2 = 0; q2 < k; ++q2) skip |= (nb[q2] == c);
-          for (int q2 = 0; q2 < cnt && !skip; ++q2) skip |= (out[q2] == c);
-          if (skip) continue;
-          out[cnt++] = c;
-        }
-      for (int i = cnt; i < MAXC; ++i) out[i] = -1;
-      ccnt[rl] = cnt;
-    }
-    // K5: distances (-1 for empty slots)
-    for (size_t rl = 0; rl < B; ++rl)
-      for (int s = 0; s < MAXC; ++s)
-        cdist[rl * MAXC + s] =
-            s < ccnt[rl] ? dist_of(S, row0 + rl, (size_t)cand[rl * MAXC + s]) : -1.0f;
-    // K6: forward merge; -1 sentinels sort first and stop the merge, so only
-    // rows with all 256 slots valid change (insertion_kernel.cuh:407-534)
-    for (size_t rl = 0; rl < B; ++rl) {
-      const int *ci = &cand[rl * MAXC];
-      const float *cd = &cdist[rl * MAXC];
-      int sid[W];
-      float sd[W];
+  if (S.precision == 1) {
+    // exact lists: the 32 smallest (dist, id) keys over the inserted rows
+    const size_t n_eff = row0 + B;
+    for (size_t r = row0; r < row0 + B; ++r) {
+      std::vector<std::pair<float, int>> all;
+      for (size_t j = 0; j < n_eff; ++j)
+        if (j != r) all.push_back({dist_of(S, r, j), (int)j});
+      const size_t m = std::min<size_t>(W, all.size());
+      std::partial_sort(all.begin(), all.begin() + (long)m, all.end());
       for (int i = 0; i < W; ++i) {
-        sid[i] = -1;
-        sd[i] = -1.0f;
-      }
-      int filled = 0;
-      for (int i = 0; i < MAXC; ++i) {
-        const int id = ci[i];
-        const float dv = cd[i];
-        if (filled >= W && dv >= sd[W - 1]) continue;
-        int pos = filled < W ? filled : W - 1;
-        while (pos > 0 && (dv < sd[pos - 1] || (dv == sd[pos - 1] && id < sid[pos - 1]))) {
-          sid[pos] = sid[pos - 1];
-          sd[pos] = sd[pos - 1];
-          --pos;
-        }
-        sid[pos] = id;
-        sd[pos] = dv;
-        if (filled < W) ++filled;
-      }
-      int *li = &S.gid[(row0 + rl) * W];
-      float *lf = &S.gd[(row0 + rl) * W];
-      int nl[W];
-      float nd[W];
-      std::memcpy(nl, li, sizeof(nl));
-      std::memcpy(nd, lf, sizeof(nd));
-      bool upd = false;
-      for (int i = 0; i < W; ++i) {
-        const int id = sid[i];
-        const float dv = sd[i];
-        bool in = false;
-        for (int q2 = 0; q2 < W; ++q2) in |= (nl[q2] == id);
-        if (in) continue;
-        if (dv > nd[W - 1] || dv < 0.0f || (dv == nd[W - 1] && id >= nl[W - 1])) break;
-        int pos = W - 1;
-        while (pos > 0 && (dv < nd[pos - 1] || (dv == nd[pos - 1] && id < nl[pos - 1]))) {
-          nl[pos] = nl[pos - 1];
-          nd[pos] = nd[pos - 1];
-          --pos;
-        }
-        nl[pos] = id;
-        nd[pos] = dv;
-        upd = true;
-      }
-      if (upd) {
-        std::memcpy(li, nl, sizeof(nl));
-        std::memcpy(lf, nd, sizeof(nd));
+        S.gid[r * W + i] = i < (int)m ? all[i].second : SENT;
+        S.gd[r * W + i] = i < (int)m ? all[i].first : FLT_MAX;
       }
     }
-    // K7/K8: reverse offers into existing rows (< row0)
-    if (row0 > 0)
+    for (size_t j = 0; j < row0; ++j)
+      for (size_t r = row0; r < row0 + B; ++r)
+        if (list_offer(&S.gid[j * W], &S.gd[j * W], (int)r, dist_of(S, j, r)) < W) S.dirty[j] = 1;
+  } else {
+    // K3: random initial neighbours (insertion_kernel.cuh:170-248)
+    for (size_t r = row0; r < row0 + B; ++r) {
+      int *ids = &S.gid[r * W];
+      float *ds = &S.gd[r * W];
+      for (int i = 0; i < W; ++i) {
+        ids[i] = SENT;
+        ds[i] = FLT_MAX;
+      }
+      if (n <= 1) continue;
+      Rng g;
+      rng_init(g, seed, (uint32_t)r, TAG_INIT_NB);
+      const int max_fill = std::min(W, n - 1);
+      const int wsize = n - wstart;
+      const int quota = std::min(W / 2, std::max(0, wsize - 1));
+      std::vector<int> f;
+      auto has = [&](int c) { return std::find(f.begin(), f.end(), c) != f.end(); };
+      int att = 0;
+      while ((int)f.size() < quota && att < quota * 16) {
+        ++att;
+        const int c = wstart + (int)(rng_next(g) % (uint32_t)wsize);
+        if (c == (int)r || has(c)) continue;
+        f.push_back(c);
+      }
+      for (uint32_t t = 0; (int)f.size() < max_fill && t < (1u << 20); ++t) {
+        const int c = (int)(rng_next(g) % (uint32_t)n);
+        if (c == (int)r || has(c)) continue;
+        f.push_back(c);
+      }
+      for (int c = 0; (int)f.size() < max_fill && c < n; ++c)
+        if (c != (int)r && !has(c)) f.push_back(c);
+      for (size_t i = 0; i < f.size(); ++i) ids[i] = f[i];
+    }
+    std::vector<int> cand(B * MAXC), ccnt(B);
+    std::vector<float> cdist(B * MAXC);
+    for (int it = 0; it < 10; ++it) {
+      // K4: two-hop candidates (insertion_kernel.cuh:250-321)
+      for (size_t rl = 0; rl < B; ++rl) {
+        const int g = (int)(row0 + rl);
+        int nb[W];
+        for (int j = 0; j < k; ++j) {
+          const int e = S.gid[(size_t)g * W + j];
+          nb[j] = (e >= 0 && e < n) ? e : SENT;
+        }
+        int *out = &cand[rl * MAXC];
+        int cnt = 0;
+        for (int kk = 0; kk < k && cnt < MAXC; ++kk)
+          for (int j = 0; j < k && cnt < MAXC; ++j) {
+            if (nb[j] == SENT) continue;
+            const int c = S.gid[(size_t)nb[j] * W + kk];
+            if ((uint32_t)c >= (uint32_t)n || c == g) continue;
+            bool skip = false;
+            for (int q2 = 0; q2 < k; ++q2) skip |= (nb[q2] == c);
+            for (int q2 = 0; q2 < cnt && !skip; ++q2) skip |= (out[q2] == c);
+            if (skip) continue;
+            out[cnt++] = c;
+          }
+        for (int i = cnt; i < MAXC; ++i) out[i] = -1;
+        ccnt[rl] = cnt;
+      }
+      // K5: distances (-1 for empty slots)
       for (size_t rl = 0; rl < B; ++rl)
-        for (int s = 0; s < ccnt[rl]; ++s) {
-          const int j = cand[rl * MAXC + s];
-          const float dv = cdist[rl * MAXC + s];
-          if (j < 0 || (size_t)j >= row0 || dv < 0.0f) continue;
-          if (list_offer(&S.gid[(size_t)j * W], &S.gd[(size_t)j * W], (int)(row0 + rl), dv) < W)
-            S.dirty[j] = 1;
+        for (int s = 0; s < MAXC; ++s)
+          cdist[rl * MAXC + s] =
+              s < ccnt[rl] ? dist_of(S, row0 + rl, (size_t)cand[rl * MAXC + s]) : -1.0f;
+      // K6: forward merge; -1 sentinels sort first and stop the merge, so only
+      // rows with all 256 slots valid change (insertion_kernel.cuh:407-534)
+      for (size_t rl = 0; rl < B; ++rl) {
+        const int *ci = &cand[rl * MAXC];
+        const float *cd = &cdist[rl * MAXC];
+        int sid[W];
+        float sd[W];
+        for (int i = 0; i < W; ++i) {
+          sid[i] = -1;
+          sd[i] = -1.0f;
         }
+        int filled = 0;
+        for (int i = 0; i < MAXC; ++i) {
+          const int id = ci[i];
+          const float dv = cd[i];
+          if (filled >= W && dv >= sd[W - 1]) continue;
+          int pos = filled < W ? filled : W - 1;
+          while (pos > 0 && (dv < sd[pos - 1] || (dv == sd[pos - 1] && id < sid[pos - 1]))) {
+            sid[pos] = sid[pos - 1];
+            sd[pos] = sd[pos - 1];
+            --pos;
+          }
+          sid[pos] = id;
+          sd[pos] = dv;
+          if (filled < W) ++filled;
+        }
+        int *li = &S.gid[(row0 + rl) * W];
+        float *lf = &S.gd[(row0 + rl) * W];
+        int nl[W];
+        float nd[W];
+        std::memcpy(nl, li, sizeof(nl));
+        std::memcpy(nd, lf, sizeof(nd));
+        bool upd = false;
+        for (int i = 0; i < W; ++i) {
+          const int id = sid[i];
+          const float dv = sd[i];
+          bool in = false;
+          for (int q2 = 0; q2 < W; ++q2) in |= (nl[q2] == id);
+          if (in) continue;
+          if (dv > nd[W - 1] || dv < 0.0f || (dv == nd[W - 1] && id >= nl[W - 1])) break;
+          int pos = W - 1;
+          while (pos > 0 && (dv < nd[pos - 1] || (dv == nd[pos - 1] && id < nl[pos - 1]))) {
+            nl[pos] = nl[pos - 1];
+            nd[pos] = nd[pos - 1];
+            --pos;
+          }
+          nl[pos] = id;
+          nd[pos] = dv;
+          upd = true;
+        }
+        if (upd) {
+          std::memcpy(li, nl, sizeof(nl));
+          std::memcpy(lf, nd, sizeof(nd));
+        }
+      }
+      // K7/K8: reverse offers into existing rows (< row0)
+      if (row0 > 0)
+        for (size_t rl = 0; rl < B; ++rl)
+          for (int s = 0; s < ccnt[rl]; ++s) {
+            const int j = cand[rl * MAXC + s];
+            const float dv = cdist[rl * MAXC + s];
+            if (j < 0 || (size_t)j >= row0 || dv < 0.0f) continue;
+            if (list_offer(&S.gid[(size_t)j * W], &S.gd[(size_t)j * W], (int)(row0 + rl), dv) < W)
+              S.dirty[j] = 1;
+          }
+    }
   }
   // CPU diff + publish (insertion_kernel.cuh:1034-1089; impl.cuh:103-144)
   std::vector<uint32_t> affected;
@@ -968,7 +988,7 @@ struct gmo_session {
 };
 
 gmo_session *gmo_create(uint64_t n_instances, uint64_t n_features, int k, int metric, float a,
-                        float b, float alpha, int neg_rate, int max_epoch) {
+                        float b, float alpha, int neg_rate, int max_epoch, int precision) {
   if (k < 1 || k > 32 || n_features < 1) return nullptr;
   auto *o = new gmo_session();
   Session &S = o->s;
@@ -982,6 +1002,7 @@ gmo_session *gmo_create(uint64_t n_instances, uint64_t n_features, int k, int me
   S.alpha = alpha;
   S.neg_rate = neg_rate;
   S.max_epoch = max_epoch;
+  S.precision = precision;
   const size_t N = std::max<size_t>(n_instances, 1);
   S.X.assign(N * S.ld, 0.0f);
   S.norms.assign(N, 0.0f);

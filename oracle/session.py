@@ -21,7 +21,8 @@ def load() -> C.CDLL:
         build_oracle()
     lib = C.CDLL(str(p))
     sig = {
-        "gmo_create": (_P, [C.c_uint64, C.c_uint64, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int]),
+        "gmo_create": (_P, [C.c_uint64, C.c_uint64, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int,
+                            C.c_int]),
         "gmo_destroy": (None, [_P]),
         "gmo_append": (C.c_int, [_P, _P, C.c_uint64, C.c_uint64]),
         "gmo_run": (C.c_int, [_P, C.c_uint32, C.c_uint32, C.c_uint32, _P]),
@@ -62,11 +63,11 @@ BUF = {"graph_ids": 0, "graph_dists": 1, "knn_ids": 2, "knn_dists": 3, "norms": 
 
 class OracleSession:
     def __init__(self, n_instances, n_features, k=15, metric=0, a=1.0, b=1.0, alpha=1.0,
-                 negative_sample_rate=5, max_epoch=200):
+                 negative_sample_rate=5, max_epoch=200, precision=0):
         self._lib = load()
         self.n_instances, self.n_features, self.k = n_instances, n_features, k
         self._h = self._lib.gmo_create(n_instances, n_features, k, metric, a, b, alpha,
-                                       negative_sample_rate, max_epoch)
+                                       negative_sample_rate, max_epoch, precision)
         if not self._h:
             raise ValueError("bad oracle parameters")
         self.ld = (n_features + 3) // 4 * 4

@@ -193,3 +193,43 @@ def test_errors_and_edge_cases(native):
     with pytest.raises(native.GMError) as e:
         s.run(1, 1, 1)
     assert e.value.code == native.GM_ERR_CLOSED
+
+
+# ---------------------------------------------------------------------------
+# precision 1: exact insertion on BF16 tensor-core tiles + FP32 re-score
+# ---------------------------------------------------------------------------
+def test_exact_distance_tile_accuracy(native):
+    n, d = 1000, 100
+    X, _ = gaussian_mixture(n, d, seed=5)
+    s = native.Session(native.default_params(n_instances=n, n_features=d, device=0, precision=1))
+    s.append_host(X)
+    s.run(n, 0, 0)
+    D = s.copy("exact_d", F32)[: n * n].reshape(n, n)
+    x = X.astype(np.float64)
+    sq = (x * x).sum(1)
+    ref = sq[:, None] + sq[None, :] - 2.0 * x @ x.T
+    bound = 0.009 * np.sqrt(np.outer(sq, sq)) + 1e-6 * (sq[:, None] + sq[None, :])
+    err = np.abs(D - ref)
+    assert np.all(err <= bound), float((err / bound).max())
+    # the tile really is BF16: errors are present, and far above FP32 rounding
+    assert err.mean() > 1e-4 * np.abs(ref).mean()
+
+
+@pytest.mark.parametrize("d,metric,k", [(24, 0, 15), (100, 0, 15), (130, 1, 10), (784, 0, 15)])
+def test_exact_mode_bitexact(native, oracle_mod, d, metric, k):
+    n = 3000 if d < 784 else 2400
+    X, _ = gaussian_mixture(n, d, seed=d)
+    s, o = pair(native, oracle_mod, n, d, k=k, metric=metric, max_epoch=20)
+    s = native.Session(native.default_params(n_instances=n, n_features=d, n_neighbors=k, metric=metric,
+                                             max_epoch=20, device=0, precision=1))
+    o = oracle_mod.OracleSession(n, d, k=k, metric=metric, max_epoch=20, precision=1)
+    step = n // 4
+    for c in range(4):
+        chunk = X[c * step : (c + 1) * step]
+        s.append_host(chunk)
+        o.append(chunk)
+        same_result(s.run(step, 300, 400), o.run(step, 300, 400))
+        same_state(s, o, embed=True, tag=f"exact cycle {c}")
+    ei, _ = exact_knn(X, k, metric="cosine" if metric else "euclidean")
+    idx = s.copy("pub_idx", U32).reshape(n, k + 1)[:, :k]
+    assert recall_at_k(idx, ei) > 0.99

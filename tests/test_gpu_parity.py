@@ -219,7 +219,6 @@ def test_exact_distance_tile_accuracy(native):
 def test_exact_mode_bitexact(native, oracle_mod, d, metric, k):
     n = 3000 if d < 784 else 2400
     X, _ = gaussian_mixture(n, d, seed=d)
-    s, o = pair(native, oracle_mod, n, d, k=k, metric=metric, max_epoch=20)
     s = native.Session(native.default_params(n_instances=n, n_features=d, n_neighbors=k, metric=metric,
                                              max_epoch=20, device=0, precision=1))
     o = oracle_mod.OracleSession(n, d, k=k, metric=metric, max_epoch=20, precision=1)

@@ -8,13 +8,17 @@ until recall@15 on 2,000 seeded query rows (against an exact FP64 brute
 force computed before timing) reaches 0.95; the recall checks are inside the
 timed region, as the metric counts every cycle until the target is met.
 
-* ``value``  -- the C ABI with the input already resident in HBM
-  (gm_append_device), CUDA-event timed on the device.
+* ``value``  -- precision 1 (BF16 tensor-core distance tiles, FP32 re-score:
+  the precision form of this workload) through the C ABI with the input
+  already resident in HBM (gm_append_device), timed with CUDA events.
+* ``plain_fp32`` -- the reference's own algorithm (precision 0, FP32
+  NN-Descent) on the same workload and clock, for comparison.
 * ``e2e``    -- the public Python API (gpumap_gb300.GPUMAP over pinned host
   chunks; every cycle copies its 500 rows host->device, each step ends by
   reading the k-NN table back to the host).
-* ``roofline`` -- the local-join kernel's algorithmic bytes over its own
-  CUDA-event time (events recorded by the engine on its stream).
+* ``roofline`` -- the kernel with the largest summed time, its algorithmic
+  bytes (or FLOPs) over its CUDA-event time (events recorded by the engine on
+  its own stream), against MEASURED_PEAKS.json.
 * ``cpu_baseline`` / ``--impl reference`` -- the CPU restatement of the
   reference path (oracle/) on a bounded sample of the same workload.
 
@@ -54,12 +58,15 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--update-ops", type=int, default=UPD_OPS)
+    ap.add_argument("--precision", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--update-ops", type=int, default=None,
+                    help="U per cycle (default 0 for precision 1, 2000 for precision 0)")
     ap.add_argument("--embedding-ops", type=int, default=EMB_OPS)
     ap.add_argument("--max-final-updates", type=int, default=MAX_FINAL_UPDATE_CYCLES)
     ap.add_argument("--n-points", type=int, default=N_POINTS)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
     return ap.parse_args()
 
 
@@ -162,11 +169,11 @@ def flush_l2(buf):
     buf.zero_()
 
 
-def run_value_step(native, X_dev, n, d, upd, emb, max_final, stats_on, q_idx, exact):
+def run_value_step(native, X_dev, n, d, upd, emb, max_final, stats_on, q_idx, exact, precision):
     import torch
 
     p = native.default_params(n_instances=n, n_features=d, n_neighbors=K, max_epoch=MAX_EPOCH,
-                              device=torch.cuda.current_device())
+                              device=torch.cuda.current_device(), precision=precision)
     p.a, p.b = 1.5769434602697652, 0.8950608778515733  # find_ab_params(1.0, 0.1)
     s = native.Session(p)
     s.set_stats(stats_on)
@@ -203,7 +210,7 @@ class _Cai:
                                          "strides": (cols * esz, esz), "data": (ptr, False)}
 
 
-def run_e2e_step(X_host, n, d, upd, emb, max_final, q_idx, exact):
+def run_e2e_step(X_host, n, d, upd, emb, max_final, q_idx, exact, precision):
     import torch
 
     import gpumap_gb300 as gm
@@ -214,6 +221,7 @@ def run_e2e_step(X_host, n, d, upd, emb, max_final, q_idx, exact):
     params = gm.GPUMAPParams()
     params.n_instances, params.n_features, params.n_neighbors = n, d, K
     params.max_epoch = MAX_EPOCH
+    params.precision = precision
     model = gm.GPUMAP(ArrayDataLoader(X_host), params)
     for c in range(0, n, CHUNK):
         model.run_with_n_ops(min(CHUNK, n - c), upd, emb)
@@ -246,6 +254,38 @@ def cpu_baseline_sample(X, upd, emb, cycles=2):
     return n / dt, dt, n
 
 
+def roofline(stats, d, peaks):
+    """Per-kernel achieved rates; returns (dominant name, dict of all)."""
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    tflops = peaks.get("bf16_tflops_sustained", 1700.0)
+    agg = {}
+
+    def add(name, ms, work, launches, bound):
+        if ms <= 0 or launches <= 0:
+            return
+        rate = (work / launches) / ((ms / launches) / 1000.0)
+        if bound == "tensor":
+            ach, peak, unit = rate / 1e12, tflops, "TFLOP/s"
+        else:
+            ach, peak, unit = rate / 1e9, hbm, "GB/s"
+        agg[name] = {"bound": bound, "achieved": ach, "peak": peak, "unit": unit, "frac": ach / peak,
+                     "ms": ms, "launches": launches}
+
+    st = {k: sum(getattr(s_, k) for s_ in stats) for k in (
+        "exact_ms", "exact_flops", "exact_launches", "screen_ms", "exact_rescored", "exact_pairs",
+        "join_ms", "join_rows", "join_pairs", "join_launches", "cand_ms", "cand_rows", "cand_launches",
+        "sgd_ms", "sgd_edges", "sgd_negatives", "sgd_launches")}
+    add("k_exact_dist", st["exact_ms"], st["exact_flops"], st["exact_launches"], "tensor")
+    add("exact_screen", st["screen_ms"], st["exact_rescored"] * 2 * d * 4 + st["exact_pairs"] * 8,
+        st["exact_launches"], "hbm")
+    add("k_local_join", st["join_ms"], st["join_rows"] * d * 4 + st["join_pairs"] * 8, st["join_launches"], "hbm")
+    add("k_candidate_dists", st["cand_ms"], st["cand_rows"] * d * 4, st["cand_launches"], "hbm")
+    add("k_sgd_epoch (200 per launch)", st["sgd_ms"], st["sgd_edges"] * 28 + (st["sgd_edges"] + st["sgd_negatives"]) * 8,
+        st["sgd_launches"], "hbm")
+    dom = max(agg, key=lambda k: agg[k]["ms"]) if agg else None
+    return dom, agg
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
@@ -253,30 +293,34 @@ def main():
 
     n, d = args.n_points, N_FEATURES
     X, _ = image_like(n, d, seed=0)
+    upd = args.update_ops if args.update_ops is not None else (0 if args.precision == 1 else UPD_OPS)
+    emb = args.embedding_ops
     config = {"workload": f"image-like mixture {n}x{d}, k={K}, euclidean, {CHUNK} points/cycle, "
-                          f"run_with_n_ops({CHUNK},{args.update_ops},{args.embedding_ops}) per cycle, then "
+                          f"run_with_n_ops({CHUNK},{upd},{emb}) per cycle, then "
                           f"run_with_n_ops(0,{n},0) until recall@15>={RECALL_TARGET}",
               "n_points": n, "n_features": d, "n_neighbors": K, "max_epoch": MAX_EPOCH,
-              "update_ops": args.update_ops, "embedding_ops": args.embedding_ops,
+              "precision": args.precision, "update_ops": upd, "embedding_ops": emb,
               "l2": "inputs (220 MB) larger than L2; 512 MB flush between steps",
-              "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+              "parallelism": "replicas" if world > 1 else "single GPU"}
 
     if args.impl == "reference":
         if rank != 0:
             return
         steps = []
         for i in range(args.warmup + args.steps):
-            v, dt, npts = cpu_baseline_sample(X, args.update_ops, args.embedding_ops, cycles=1)
+            v, dt, npts = cpu_baseline_sample(X, UPD_OPS, emb, cycles=1)
             if i >= args.warmup:
                 steps.append((v, dt))
         val = statistics.median([v for v, _ in steps])
         line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "points/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * statistics.median([t for _, t in steps]),
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": config,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000 * statistics.median([t for _, t in steps]),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": config,
                 "cpu_baseline": {"value": val, "unit": "points/s", "cores": 1, "kind": "port",
-                                 "sample": f"first {CHUNK} rows, one cycle run_with_n_ops({CHUNK},{args.update_ops},{args.embedding_ops}); "
-                                           "the reference's CUDA build is unavailable (needs RAFT/RMM, CUDA 12.6)"},
+                                 "sample": f"first {CHUNK} rows, one cycle run_with_n_ops({CHUNK},{UPD_OPS},{emb}) of "
+                                           "the reference algorithm on one host thread; the reference's CUDA build "
+                                           "is unavailable (needs RAFT/RMM and CUDA 12.6)"},
                 "e2e": {"value": val, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -299,72 +343,72 @@ def main():
     q_idx = np.random.default_rng(123).choice(n, min(RECALL_QUERIES, n), replace=False)
     exact = exact_knn_gpu(X_dev, q_idx, K)
 
+    def step(precision, u, stats_on):
+        return run_value_step(native, X_dev, n, d, u, emb, args.max_final_updates, stats_on, q_idx, exact,
+                              precision)
+
     for _ in range(args.warmup):
-        s, _, _, _, _ = run_value_step(native, X_dev, n, d, args.update_ops, args.embedding_ops,
-                                       args.max_final_updates, False, q_idx, exact)
+        s, _, _, _, _ = step(args.precision, upd, False)
         del s
     barrier(world)
-    times, recalls, rounds_l, launches, join = [], [], [], 0, []
+    times, recalls, rounds_l, launches, stats = [], [], [], 0, []
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             flush_l2(flush)
             torch.cuda.synchronize()
             barrier(world)
-            s, ms, st, rec, rounds = run_value_step(native, X_dev, n, d, args.update_ops, args.embedding_ops,
-                                                    args.max_final_updates, True, q_idx, exact)
+            s, ms, st, rec, rounds = step(args.precision, upd, True)
             times.append(ms)
             rounds_l.append(rounds)
             launches += st.kernel_launches
-            join.append((st.join_ms, st.join_rows, st.join_pairs, st.join_launches, st.cand_ms, st.cand_rows,
-                         st.cand_launches, st.sgd_ms, list(st.phase_s)))
+            stats.append(st)
             recalls.append(rec)
             del s
     total_ms = max_over_ranks(sum(times), world)
     ms_step = total_ms / args.steps
     value = world * n * args.steps / (total_ms / 1000.0)
 
-    # roofline: local join (dominant update kernel) and candidate distances
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
-    hbm = peaks.get("hbm_gbs", 6800.0)
-    j_ms = sum(j[0] for j in join)
-    j_bytes = sum(j[1] * d * 4 + j[2] * 8 for j in join)
-    c_ms = sum(j[4] for j in join)
-    c_bytes = sum(j[5] * d * 4 for j in join)
-    j_launch = sum(j[3] for j in join)
-    c_launch = sum(j[6] for j in join)
-    dominant = "local_join" if j_ms >= c_ms else "candidate_dists"
-    if dominant == "local_join":
-        ach = (j_bytes / max(j_launch, 1)) / ((j_ms / max(j_launch, 1)) / 1000.0) / 1e9 if j_ms > 0 else 0.0
-    else:
-        ach = (c_bytes / max(c_launch, 1)) / ((c_ms / max(c_launch, 1)) / 1000.0) / 1e9 if c_ms > 0 else 0.0
-    traffic_path = ROOT / "profiles" / "traffic.json"
-    traffic = None
-    if traffic_path.exists():
-        traffic = json.loads(traffic_path.read_text()).get(dominant)
+    dom, kernels = roofline(stats, d, peaks)
+    roof = dict(kernels[dom]) if dom else {}
+    if dom:
+        roof = {"kernel": dom, "bound": roof["bound"], "achieved": roof["achieved"], "peak": roof["peak"],
+                "unit": roof["unit"], "frac": roof["frac"], "traffic": None,
+                "peak_source": "measured (MEASURED_PEAKS.json, sustained bf16 / hbm copy)"}
     line = {
         "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded image-like mixture, 70k x 784)",
-        "config": config,
+        "vs_baseline": None, "dtype": "bf16+f32" if args.precision == 1 else "f32",
+        "data": "synthetic (seeded image-like mixture, 70k x 784)", "config": config,
         "recall_at_15": min(recalls), "recall_valid": min(recalls) >= RECALL_TARGET,
-        "final_update_cycles": rounds_l,
-        "gpu_launches": int(launches),
-        "roofline": {"kernel": dominant, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
-                     "frac": ach / hbm if hbm else None, "traffic": traffic, "peak_source": "measured"},
-        "kernel_time_ms": {"local_join": j_ms / args.steps, "candidate_dists": c_ms / args.steps,
-                           "sgd": sum(j[7] for j in join) / args.steps},
-        "phase_s": [sum(j[8][i] for j in join) / args.steps for i in range(3)],
+        "final_update_cycles": rounds_l, "gpu_launches": int(launches),
+        "roofline": roof,
+        "kernels": {k: {kk: (round(vv, 4) if isinstance(vv, float) else vv) for kk, vv in v.items()}
+                    for k, v in kernels.items()},
+        "phase_s": [sum(s_.phase_s[i] for s_ in stats) / args.steps for i in range(3)],
     }
     line["clocks"] = clk.summary()
 
+    if args.precision == 1 and not args.no_plain:
+        s, _, _, _, _ = step(0, UPD_OPS, False)
+        del s
+        flush_l2(flush)
+        s, ms0, _, rec0, rounds0 = step(0, UPD_OPS, False)
+        del s
+        line["plain_fp32"] = {"value": n / (ms0 / 1000.0), "unit": "points/s", "recall_at_15": rec0,
+                              "recall_valid": rec0 >= RECALL_TARGET, "final_update_cycles": rounds0,
+                              "schedule": f"run_with_n_ops({CHUNK},{UPD_OPS},{emb}) then up to "
+                                          f"{args.max_final_updates} full update cycles",
+                              "note": "the reference's NN-Descent (precision 0); it plateaus below the recall "
+                                      "target on this workload"}
+
     if not args.no_e2e:
         X_pin = torch.from_numpy(X).pin_memory().numpy()
-        run_e2e_step(X_pin, n, d, args.update_ops, args.embedding_ops, args.max_final_updates, q_idx, exact)
+        run_e2e_step(X_pin, n, d, upd, emb, args.max_final_updates, q_idx, exact, args.precision)
         e2e_t, e2e_rec = [], []
         for _ in range(max(1, min(args.steps, 3))):
             flush_l2(flush)
-            dt, rec, _ = run_e2e_step(X_pin, n, d, args.update_ops, args.embedding_ops, args.max_final_updates,
-                                      q_idx, exact)
+            dt, rec, _ = run_e2e_step(X_pin, n, d, upd, emb, args.max_final_updates, q_idx, exact, args.precision)
             e2e_t.append(dt)
             e2e_rec.append(rec)
         tmax = max_over_ranks(sum(e2e_t), world)
@@ -372,10 +416,10 @@ def main():
                        "h2d_bytes_per_step": n * d * 4, "d2h_bytes_per_step": n * K * 4,
                        "recall_at_15": min(e2e_rec)}
     if rank == 0 and not args.no_cpu_baseline:
-        v, dt, npts = cpu_baseline_sample(X, args.update_ops, args.embedding_ops, cycles=2)
+        v, dt, npts = cpu_baseline_sample(X, UPD_OPS, emb, cycles=2)
         line["cpu_baseline"] = {"value": v, "unit": "points/s", "cores": 1, "kind": "port",
                                 "sample": f"first {npts} rows in {npts // CHUNK} cycles of run_with_n_ops({CHUNK},"
-                                          f"{args.update_ops},{args.embedding_ops}), {dt:.1f} s, CPU restatement"}
+                                          f"{UPD_OPS},{emb}) of the reference algorithm, {dt:.1f} s, one host thread"}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -59,8 +59,10 @@ class gm_stats(C.Structure):
         ("join_nodes", C.c_uint64), ("join_rows", C.c_uint64), ("join_pairs", C.c_uint64),
         ("join_merges", C.c_uint64), ("cand_launches", C.c_uint64), ("cand_ms", C.c_double),
         ("cand_rows", C.c_uint64), ("sgd_launches", C.c_uint64), ("sgd_ms", C.c_double),
-        ("exact_launches", C.c_uint64), ("exact_ms", C.c_double), ("exact_pairs", C.c_uint64),
-        ("exact_rescored", C.c_uint64), ("phase_s", C.c_double * 3),
+        ("sgd_edges", C.c_uint64), ("sgd_negatives", C.c_uint64),
+        ("exact_launches", C.c_uint64), ("exact_ms", C.c_double), ("exact_flops", C.c_double),
+        ("screen_ms", C.c_double), ("exact_pairs", C.c_uint64), ("exact_rescored", C.c_uint64),
+        ("phase_s", C.c_double * 3),
     ]
 
 

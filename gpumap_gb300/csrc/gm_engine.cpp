@@ -88,7 +88,7 @@ Session::Session(const gm_params &p) : p_(p) {
     st_.emb = (float *)dalloc(Nm * 2 * sizeof(float));
     st_.bloom = (uint32_t *)dalloc(Nm * 64 * sizeof(uint32_t));
     st_.err = (unsigned *)dalloc(16);
-    d_stat_ = (unsigned long long *)dalloc(8 * sizeof(unsigned long long));
+    d_stat_ = (unsigned long long *)dalloc(16 * sizeof(unsigned long long));
     st_.stat = d_stat_;
 
     us_.fwd_new = (int *)dalloc(Nm * kSamples * sizeof(int));
@@ -157,7 +157,7 @@ Session::Session(const gm_params &p) : p_(p) {
   ck(cudaMemsetAsync(st_.emb, 0, Nm * 2 * sizeof(float), s), "memset");
   ck(cudaMemsetAsync(st_.bloom, 0, Nm * 64 * sizeof(uint32_t), s), "memset");
   ck(cudaMemsetAsync(st_.err, 0, 16, s), "memset");
-  ck(cudaMemsetAsync(d_stat_, 0, 8 * sizeof(unsigned long long), s), "memset");
+  ck(cudaMemsetAsync(d_stat_, 0, 16 * sizeof(unsigned long long), s), "memset");
   ck(cudaMemsetAsync(us_.sizes, 0, Nm * sizeof(int4), s), "memset");
   ck(cudaMemsetAsync(es_.sigma, 0, Nm * sizeof(float), s), "memset");
   ck(cudaMemsetAsync(es_.rho, 0, Nm * sizeof(float), s), "memset");
@@ -313,6 +313,8 @@ void Session::collect_timings() {
       } else if (pr.slot == 3) {
         stats_.exact_ms += ms;
         stats_.exact_launches += 1;
+      } else if (pr.slot == 4) {
+        stats_.screen_ms += ms;
       }
     }
     ev_pool_.push_back(pr.a);
@@ -325,7 +327,7 @@ void Session::reset_stats() {
   sync();
   collect_timings();
   stats_ = gm_stats{};
-  cudaMemsetAsync(d_stat_, 0, 8 * sizeof(unsigned long long), stream_);
+  cudaMemsetAsync(d_stat_, 0, 16 * sizeof(unsigned long long), stream_);
   launch_counter_reset();
   sync();
 }
@@ -333,7 +335,7 @@ void Session::reset_stats() {
 void Session::get_stats(gm_stats *out) {
   sync();
   collect_timings();
-  unsigned long long h[8];
+  unsigned long long h[16];
   ck(cudaMemcpy(h, d_stat_, sizeof(h), cudaMemcpyDeviceToHost), "stats");
   stats_.join_nodes = h[0];
   stats_.join_rows = h[1];
@@ -342,6 +344,8 @@ void Session::get_stats(gm_stats *out) {
   stats_.cand_rows = h[4];
   stats_.exact_pairs = h[5];
   stats_.exact_rescored = h[6];
+  stats_.sgd_edges = h[7];
+  stats_.sgd_negatives = h[8];
   stats_.kernel_launches = launch_counter();
   *out = stats_;
 }
@@ -447,15 +451,20 @@ uint32_t Session::insert(uint32_t n_ops) {
     // exact lists: every batch row against every inserted row on the tensor
     // cores, re-scored in FP32 where the BF16 bound cannot decide
     launch_to_bf16(st_, xh_, dh_, row0, nb, s);
-    timed_begin(3);
+    // columns: the rows inserted so far (rows appended but still queued have
+    // no norms or shadow rows yet)
+    const int ncol = row0 + nb;
     for (int b0 = 0; b0 < nb; b0 += ex_block_) {
       const int rows = std::min(ex_block_, nb - b0);
-      // columns: the rows inserted so far (rows appended but still queued
-      // have no norms or shadow rows yet)
-      launch_exact_block(st_, maps_, dh_, row0, b0, rows, row0 + nb, ex_D_, (long)(row0 + nb),
-                         ex_cand_, (long)(row0 + nb), sms_, s);
+      timed_begin(3);
+      launch_exact_dist(st_, maps_, dh_, row0, b0, rows, ncol, ex_D_, (long)ncol, sms_, s);
+      timed_end(3);
+      timed_begin(4);
+      launch_exact_screen(st_, row0, b0, rows, ncol, ex_D_, (long)ncol, ex_cand_, (long)ncol, s);
+      timed_end(4);
+      const uint64_t flops = 2ull * (uint64_t)rows * (uint64_t)ncol * (uint64_t)dh_;
+      stats_.exact_flops += (double)(stats_on_ ? flops : 0);
     }
-    timed_end(3);
   } else {
     ensure_cand(B);
     launch_random_init(st_, row0, nb, n, window_start, seed, s);
@@ -651,7 +660,7 @@ void Session::run_sgd_graph() {
     ck(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture begin");
     launch_sgd(st_.emb, es_.t_row, es_.flag_tail, es_.t_val, es_.next_s, es_.next_n, es_.iscal,
                es_.fscal, sgd_grid_, p_.alpha, 1.0f, p_.a, p_.b, (int)p_.max_epoch,
-               (int)p_.negative_sample_rate, 42ull, stream_);
+               (int)p_.negative_sample_rate, 42ull, stream_, st_.stat);
     ck(cudaStreamEndCapture(stream_, &g), "capture end");
     const cudaError_t e = cudaGraphInstantiate(&sgd_exec_, g, 0);
     cudaGraphDestroy(g);

@@ -425,9 +425,8 @@ void launch_to_bf16(const DevState &st, void *xh, int dh, int row0, int nrows, c
   note_launch();
 }
 
-void launch_exact_block(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
-                        int nrows, int n, float *D, long ldD, int *cand, long cand_ld, int sms,
-                        cudaStream_t s) {
+void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
+                       int nrows, int n, float *D, long ldD, int sms, cudaStream_t s) {
   if (nrows <= 0 || n <= 0) return;
   static unsigned configured = 0u;
   int dev = 0;
@@ -437,7 +436,6 @@ void launch_exact_block(const DevState &st, const ExactMaps &maps, int dh, int r
                          (int)kExactSmem);
     configured |= (1u << dev);
   }
-  const int brow0 = row0 + blk0;  // global first row of the block
   const int m_tiles = cdiv(nrows, kTM);
   const int n_tiles = cdiv(n, kTN);
   const int gx = std::max(1, std::min(n_tiles, std::max(1, sms / m_tiles)));
@@ -445,8 +443,14 @@ void launch_exact_block(const DevState &st, const ExactMaps &maps, int dh, int r
   memcpy(&ta, maps.a, sizeof(ta));
   memcpy(&tb, maps.b, sizeof(tb));
   k_exact_dist<<<dim3(gx, m_tiles), kExactThreads, kExactSmem, s>>>(
-      ta, tb, brow0, nrows, n, dh / kTK, st.norms, D, ldD, st.err);
+      ta, tb, row0 + blk0, nrows, n, dh / kTK, st.norms, D, ldD, st.err);
   note_launch();
+}
+
+void launch_exact_screen(const DevState &st, int row0, int blk0, int nrows, int n,
+                         const float *D, long ldD, int *cand, long cand_ld, cudaStream_t s) {
+  if (nrows <= 0 || n <= 0) return;
+  const int brow0 = row0 + blk0;  // global first row of the block
   k_exact_rows<<<cdiv(nrows, kRowWarps), kRowWarps * 32, 0, s>>>(
       D, ldD, brow0, 0, nrows, n, st.X, st.ld, st.d, st.norms, st.g_key, cand, cand_ld, st.stat);
   note_launch();

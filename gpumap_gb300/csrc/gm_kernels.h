@@ -27,7 +27,7 @@ struct DevState {
   float *emb = nullptr;        // n_cap x 2
   uint32_t *bloom = nullptr;   // n_cap x 64 words (4 sets x 512 bits)
   unsigned *err = nullptr;     // device error bits
-  unsigned long long *stat = nullptr; // device counters for statistics (8)
+  unsigned long long *stat = nullptr; // device counters for statistics (16)
 };
 
 // Update-phase scratch (capacity n_cap rows).
@@ -103,11 +103,14 @@ struct ExactMaps {
 int exact_dh(int d);  // shadow row width: d rounded up to 64
 bool make_row_maps(void *xh, int n_cap, int dh, ExactMaps *out);
 void launch_to_bf16(const DevState &st, void *xh, int dh, int row0, int nrows, cudaStream_t s);
-// Exact lists for batch rows [row0+blk0, row0+blk0+nrows) against rows [0, n),
-// and offers of those rows to rows [0, row0).  D, cand: nrows x ldD scratch.
-void launch_exact_block(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
-                        int nrows, int n, float *D, long ldD, int *cand, long cand_ld, int sms,
-                        cudaStream_t s);
+// Approximate distances D (nrows x ldD) of batch rows [row0+blk0, +nrows)
+// against rows [0, n) on the tensor cores.
+void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
+                       int nrows, int n, float *D, long ldD, int sms, cudaStream_t s);
+// Exact lists of those rows (bound, FP32 re-score, top-32) and their offers to
+// rows [0, row0).  cand: nrows x cand_ld scratch.
+void launch_exact_screen(const DevState &st, int row0, int blk0, int nrows, int n,
+                         const float *D, long ldD, int *cand, long cand_ld, cudaStream_t s);
 
 // ---- update (gm_kernels_update.cu) ----
 void launch_sample_graph(const DevState &st, const UpdScratch &u,
@@ -175,7 +178,8 @@ void launch_mark_rows(const int *rows, int nr, int *flag, cudaStream_t s);
 void launch_sgd(float *emb, const int *head, const int *tail, const float *eps,
                 float *next_s, float *next_n, const int *iscal, const float *fscal,
                 int grid, float alpha0, float gamma, float a, float b, int n_epochs,
-                int neg_rate, uint64_t seed, cudaStream_t s);
+                int neg_rate, uint64_t seed, cudaStream_t s,
+                unsigned long long *stat = nullptr);
 void launch_set_int(int *p, int v, cudaStream_t s);
 constexpr int kIscalN = 4;
 void launch_epoch_init(const float *eps, int nnz, int neg_rate, float *next_s,

@@ -263,9 +263,11 @@ GM_D float trunc_grad(float rounding, float x) {
 __global__ void k_sgd_epoch(float *emb, const int *head, const int *tail,
                             const int *iscal, const float *eps, float *next_s,
                             float *next_n, float alpha, int epoch, float gamma, float a,
-                            float b, float nsr_inv, uint64_t seed, const float *fscal) {
+                            float b, float nsr_inv, uint64_t seed, const float *fscal,
+                            unsigned long long *stat) {
   const int nnz = iscal[IS_NNZ2];
   const int n = iscal[IS_N];
+  unsigned my_edges = 0, my_negs = 0;
   const float rounding = fscal[FS_ROUND];
   const float fe = (float)epoch;
   const float bm1 = __fsub_rn(b, 1.0f);
@@ -273,6 +275,7 @@ __global__ void k_sgd_epoch(float *emb, const int *head, const int *tail,
        row += gridDim.x * blockDim.x) {
     const float ns = next_s[row];
     if (ns > fe) continue;
+    ++my_edges;
     const float ep = eps[row];
     const float ep_neg = __fmul_rn(ep, nsr_inv);
     const int j = head[row], kk = tail[row];
@@ -319,9 +322,20 @@ __global__ void k_sgd_epoch(float *emb, const int *head, const int *tail,
         g1 = __fadd_rn(g1, h1);
       }
       next_n[row] = __fadd_rn(nn, __fmul_rn((float)n_neg, ep_neg));
+      my_negs += (unsigned)n_neg;
     }
     atomicAdd(cp, trunc_grad(rounding, g0));
     atomicAdd(cp + 1, trunc_grad(rounding, g1));
+  }
+  if (stat) {
+    for (int o = 16; o > 0; o >>= 1) {
+      my_edges += __shfl_xor_sync(0xffffffffu, my_edges, o);
+      my_negs += __shfl_xor_sync(0xffffffffu, my_negs, o);
+    }
+    if ((threadIdx.x & 31) == 0 && my_edges) {
+      atomicAdd(&stat[7], (unsigned long long)my_edges);
+      atomicAdd(&stat[8], (unsigned long long)my_negs);
+    }
   }
 }
 
@@ -486,7 +500,7 @@ void launch_optimize_layout(float *emb, int n, int nb, int k, float alpha0, floa
   if (n <= 0 || n_epochs <= 0 || nb <= 0) return;
   launch_set_int(e.iscal + IS_N, n, s);
   launch_sgd(emb, e.t_row, e.flag_tail, e.t_val, e.next_s, e.next_n, e.iscal, e.fscal,
-             cdiv(2 * nb * k, 256), alpha0, gamma, a, b, n_epochs, neg_rate, seed, s);
+             cdiv(2 * nb * k, 256), alpha0, gamma, a, b, n_epochs, neg_rate, seed, s, nullptr);
 }
 
 void launch_set_int(int *p, int v, cudaStream_t s) {
@@ -505,14 +519,14 @@ void launch_epoch_init(const float *eps, int nnz, int neg_rate, float *next_s,
 void launch_sgd(float *emb, const int *head, const int *tail, const float *eps,
                 float *next_s, float *next_n, const int *iscal, const float *fscal,
                 int grid, float alpha0, float gamma, float a, float b, int n_epochs,
-                int neg_rate, uint64_t seed, cudaStream_t s) {
+                int neg_rate, uint64_t seed, cudaStream_t s, unsigned long long *stat) {
   if (n_epochs <= 0 || grid <= 0) return;
   const float nsr_inv = 1.0f / (float)neg_rate;
   float alpha = alpha0;
   uint64_t cur_seed = seed;
   for (int ep = 0; ep < n_epochs; ++ep) {
     k_sgd_epoch<<<grid, 256, 0, s>>>(emb, head, tail, iscal, eps, next_s, next_n, alpha, ep,
-                                     gamma, a, b, nsr_inv, cur_seed, fscal);
+                                     gamma, a, b, nsr_inv, cur_seed, fscal, stat);
     note_launch();
     // alpha and seed for the next epoch (reference embedding_kernel.cuh:790-792)
     alpha = alpha0 * (1.0f - (float)ep / (float)n_epochs);

@@ -92,8 +92,12 @@ typedef struct gm_stats {
   uint64_t cand_rows;         /* candidate feature rows loaded */
   uint64_t sgd_launches;
   double sgd_ms;
-  uint64_t exact_launches;    /* exact-insertion blocks (precision 1) */
-  double exact_ms;
+  uint64_t sgd_edges;         /* edge samples processed by the SGD epochs */
+  uint64_t sgd_negatives;     /* negative samples drawn */
+  uint64_t exact_launches;    /* tensor-core distance launches (precision 1) */
+  double exact_ms;            /* their summed time */
+  double exact_flops;         /* 2 x rows x columns x padded features, summed */
+  double screen_ms;           /* bound + FP32 re-score + top-32 kernels */
   uint64_t exact_pairs;       /* batch x column pairs formed on the tensor cores */
   uint64_t exact_rescored;    /* pairs re-scored in FP32 */
   double phase_s[3];          /* insertion / update / embedding seconds */

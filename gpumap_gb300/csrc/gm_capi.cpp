@@ -49,6 +49,18 @@ int ck(cudaError_t e, const char *what) {
 
 }  // namespace
 
+namespace gm {
+// Records `msg` as the calling thread's gm_last_error() (cleared for GM_OK)
+// and returns `code`; for entry points defined outside this file.
+int set_last_error(int code, const char *msg) {
+  if (code == GM_OK) {
+    g_last_error.clear();
+    return GM_OK;
+  }
+  return fail(code, msg);
+}
+}  // namespace gm
+
 extern "C" {
 
 int gm_params_default(gm_params *out) {

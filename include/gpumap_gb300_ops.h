@@ -73,6 +73,28 @@ int gm_op_sgd(float *emb, int64_t n, const int32_t *head, const int32_t *tail,
               float a, float b, int32_t n_epochs, int32_t negative_sample_rate,
               uint64_t seed, void *stream);
 
+/* Largest edge list gm_op_sgd_noalloc accepts. */
+#define GM_SGD_NOALLOC_MAX_EDGES 1048576
+
+/* gm_op_sgd without any device allocation, for callers that must not
+ * allocate while they run: a host framework whose memory pool owns the GPU
+ * (a cudaMalloc beside it can fail or fragment that pool) or a latency-bound
+ * loop that cannot take cudaFree's device-wide synchronisation.  No
+ * counterpart in the reference.  Same arguments and results as gm_op_sgd.
+ *  - Scratch is one fixed device array of 8 MiB + 128 bytes inside this
+ *    library, held by every GPU that loads it until the process exits;
+ *    nnz above GM_SGD_NOALLOC_MAX_EDGES is rejected with GM_ERR_INVALID.
+ *  - The first call on a device looks up the array's device address (with
+ *    that device current); make that first call before any stream capture.
+ *  - Every call shares the array and overwrites what it reads before use;
+ *    calls that overlap on the GPU (different streams, or threads) race.
+ *  - Returns once the work is queued on `stream`; kernel errors surface at
+ *    the caller's next synchronisation of that stream. */
+int gm_op_sgd_noalloc(float *emb, int64_t n, const int32_t *head, const int32_t *tail,
+                      const float *eps, int64_t nnz, float rounding, float alpha0, float gamma,
+                      float a, float b, int32_t n_epochs, int32_t negative_sample_rate,
+                      uint64_t seed, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

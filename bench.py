@@ -387,6 +387,9 @@ def main():
                     for k, v in kernels.items()},
         "phase_s": [sum(s_.phase_s[i] for s_ in stats) / args.steps for i in range(3)],
     }
+    if args.precision == 1:
+        line["exact_pairs_per_step"] = sum(s_.exact_pairs for s_ in stats) / args.steps
+        line["exact_rescored_per_step"] = sum(s_.exact_rescored for s_ in stats) / args.steps
     line["clocks"] = clk.summary()
 
     if args.precision == 1 and not args.no_plain:

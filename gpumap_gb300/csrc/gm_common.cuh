@@ -28,6 +28,7 @@ constexpr uint32_t kPubIdxSentinel = 0xffffffffu;
 // Device error bits, OR-ed into the session's error word.
 constexpr unsigned kDevErrLock = 1u;  // a per-node lock wait ran out
 constexpr unsigned kDevErrSpin = 2u;  // another bounded wait ran out
+constexpr unsigned kDevErrOverflow = 4u;  // a scratch pool would have overflowed (work skipped)
 
 // Lock wait bound: about a second at the longest back-off.
 constexpr uint32_t kLockSpinLimit = 1u << 20;

@@ -125,14 +125,25 @@ Session::Session(const gm_params &p) : p_(p) {
 
     ck(cudaMallocHost((void **)&h_pin_, (Nm + 64) * sizeof(uint32_t)), "cudaMallocHost");
     if (p.precision == 1) {
-      // BF16 shadow rows plus a block of distance / candidate scratch sized so
-      // that a block holds at most ~512 MB of each
+      // split-BF16 shadow rows (hi | lo, 2 x dh bf16 each) plus a block of
+      // distance / candidate scratch sized so that a block holds at most
+      // ~512 MB of each
       dh_ = exact_dh((int)d);
-      xh_ = dalloc(Nm * (size_t)dh_ * 2);
+      xh_ = dalloc(Nm * (size_t)dh_ * 4);
       ex_block_ = (int)std::max<size_t>(128, std::min<size_t>(4096, ((size_t)512 << 20) / (Nm * 4)));
       ex_block_ = ex_block_ / 128 * 128;
       ex_D_ = (float *)dalloc((size_t)ex_block_ * Nm * sizeof(float));
       ex_cand_ = (int *)dalloc((size_t)ex_block_ * Nm * sizeof(int));
+      xs_.D = ex_D_;
+      xs_.cand = ex_cand_;
+      xs_.cand_d = (float *)dalloc((size_t)ex_block_ * Nm * sizeof(float));
+      xs_.row_cnt = (int *)dalloc((size_t)ex_block_ * sizeof(int));
+      xs_.pool_cap = (long)ex_block_ * (long)Nm;
+      xs_.pool_j = (int *)dalloc((size_t)xs_.pool_cap * sizeof(int));
+      xs_.pool_m = (int *)dalloc((size_t)xs_.pool_cap * sizeof(int));
+      xs_.pool_d = (float *)dalloc((size_t)xs_.pool_cap * sizeof(float));
+      xs_.seg = (int *)dalloc(Nm * 2 * sizeof(int));
+      xs_.counter = (int *)dalloc(16 * sizeof(int));
     }
   } catch (...) {
     for (void *q : allocs_) cudaFree(q);
@@ -163,7 +174,7 @@ Session::Session(const gm_params &p) : p_(p) {
   ck(cudaMemsetAsync(es_.rho, 0, Nm * sizeof(float), s), "memset");
   ck(cudaMemsetAsync(es_.iscal, 0, 16 * sizeof(int), s), "memset");
   ck(cudaMemsetAsync(es_.fscal, 0, 16 * sizeof(float), s), "memset");
-  if (xh_) ck(cudaMemsetAsync(xh_, 0, Nm * (size_t)dh_ * 2, s), "memset");
+  if (xh_) ck(cudaMemsetAsync(xh_, 0, Nm * (size_t)dh_ * 4, s), "memset");
   ck(cudaGetLastError(), "init fill");
   ck(cudaStreamSynchronize(s), "init sync");
   if (xh_) {
@@ -449,7 +460,7 @@ uint32_t Session::insert(uint32_t n_ops) {
   launch_row_norms(st_, row0, nb, s);
   if (p_.precision == 1) {
     // exact lists: every batch row against every inserted row on the tensor
-    // cores, re-scored in FP32 where the BF16 bound cannot decide
+    // cores, re-scored in FP32 where the split-BF16 bound cannot decide
     launch_to_bf16(st_, xh_, dh_, row0, nb, s);
     // columns: the rows inserted so far (rows appended but still queued have
     // no norms or shadow rows yet)
@@ -460,9 +471,10 @@ uint32_t Session::insert(uint32_t n_ops) {
       launch_exact_dist(st_, maps_, dh_, row0, b0, rows, ncol, ex_D_, (long)ncol, sms_, s);
       timed_end(3);
       timed_begin(4);
-      launch_exact_screen(st_, row0, b0, rows, ncol, ex_D_, (long)ncol, ex_cand_, (long)ncol, s);
+      launch_exact_screen(st_, row0, b0, rows, ncol, xs_, (long)ncol, sms_, s);
       timed_end(4);
-      const uint64_t flops = 2ull * (uint64_t)rows * (uint64_t)ncol * (uint64_t)dh_;
+      // three BF16 products per padded feature (hi.hi, hi.lo, lo.hi)
+      const uint64_t flops = 6ull * (uint64_t)rows * (uint64_t)ncol * (uint64_t)dh_;
       stats_.exact_flops += (double)(stats_on_ ? flops : 0);
     }
   } else {

@@ -141,6 +141,7 @@ class Session {
   float *ex_D_ = nullptr;
   int *ex_cand_ = nullptr;
   int ex_block_ = 0;
+  ExactScreen xs_{};
   int sms_ = 0;
 
   // captured SGD epochs

@@ -1,12 +1,17 @@
 // Exact insertion (precision = 1): each insertion batch is compared with
 // every inserted row.  Distances are first formed on the 5th-generation tensor
-// cores (BF16 operands staged by TMA, FP32 accumulators in TMEM), then every
-// pair that a rigorous BF16 error bound cannot rule out is re-scored with the
+// cores (split-BF16 operands staged by TMA, FP32 accumulators in TMEM), then
+// every pair that a rigorous error bound cannot rule out is re-scored with the
 // canonical FP32 distance.  Resulting lists are the exact 32 nearest rows
 // under the canonical distance, identical to a brute-force CPU computation.
 //
-//  k_to_bf16     batch rows -> BF16 shadow rows (zero padded to a multiple of 64)
-//  k_exact_dist  approx D[m][j] = |x_m|^2 + |x_j|^2 - 2 bf16(x_m).bf16(x_j)
+// Split BF16: each FP32 value x is stored as hi = bf16(x) and lo = bf16(x - hi)
+// (x - hi is exact in FP32), and a.b is formed as hi.hi + hi.lo + lo.hi in one
+// FP32 accumulator: three BF16 products per element, relative operand error
+// about 3 * 2^-16 instead of 2^-7 for plain BF16.
+//
+//  k_to_bf16     batch rows -> [hi | lo] shadow rows (each zero padded to dh, a multiple of 64)
+//  k_exact_dist  approx D[m][j] = |x_m|^2 + |x_j|^2 - 2 (x_m . x_j)_split
 //                (tcgen05.mma kind::f16, M=128 x N=256 x K=16 per instruction)
 //  k_exact_rows  per batch row: bound, candidates, FP32 re-score, exact top-32
 //  k_exact_cols  per existing row: batch rows that may enter its list
@@ -121,7 +126,8 @@ GM_D void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// Batch rows to BF16 (round to nearest), zero padded to dh columns.
+// Batch rows to split BF16 (both halves round to nearest): shadow row =
+// hi[0..dh) | lo[0..dh), zero padded past d.
 __global__ void k_to_bf16(const float *X, int ld, int d, int dh, int row0, int nrows,
                           __nv_bfloat16 *Xh) {
   const long total = (long)nrows * dh;
@@ -130,7 +136,10 @@ __global__ void k_to_bf16(const float *X, int ld, int d, int dh, int row0, int n
     const int r = (int)(i / dh), c = (int)(i - (long)r * dh);
     const size_t row = (size_t)(row0 + r);
     const float v = c < d ? X[row * ld + c] : 0.0f;
-    Xh[row * dh + c] = __float2bfloat16_rn(v);
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(__fsub_rn(v, __bfloat162float(hi)));
+    Xh[row * 2 * dh + c] = hi;
+    Xh[row * 2 * dh + dh + c] = lo;
   }
 }
 
@@ -138,8 +147,8 @@ __global__ void k_to_bf16(const float *X, int ld, int d, int dh, int row0, int n
 // grid.y: 128-row tiles of the batch; grid.x: CTAs sharing the column tiles.
 __global__ void __launch_bounds__(kExactThreads, 1)
     k_exact_dist(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
-                 int arow0, int nb, int n, int kchunks, const float *norms, float *D, long ldD,
-                 unsigned *err) {
+                 int arow0, int nb, int n, int kchunks, int dh, const float *norms, float *D,
+                 long ldD, unsigned *err) {
   extern __shared__ __align__(1024) unsigned char raw[];
   unsigned char *base = (unsigned char *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(base + (size_t)kStages * kStageBytes);
@@ -178,16 +187,18 @@ __global__ void __launch_bounds__(kExactThreads, 1)
     if (lane == 0) {
       uint32_t it = 0;
       for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
-        for (int kc = 0; kc < kchunks; ++kc, ++it) {
+        // 3 * kchunks K steps: hi.hi, hi.lo, lo.hi (x offsets are multiples of 64)
+        for (int kc = 0; kc < 3 * kchunks; ++kc, ++it) {
           const uint32_t s = it % kStages, use = it / kStages;
           if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1)) {
             ok = false;
             break;
           }
+          const int seg = kc / kchunks, kx = (kc - seg * kchunks) * kTK;
           unsigned char *a = base + (size_t)s * kStageBytes;
           mbar_expect_tx(&full[s], kStageBytes);
-          tma_load_2d(&tm_a, &full[s], a, kc * kTK, arow0 + m0);
-          tma_load_2d(&tm_b, &full[s], a + kABytes, kc * kTK, t * kTN);
+          tma_load_2d(&tm_a, &full[s], a, (seg == 2 ? dh : 0) + kx, arow0 + m0);
+          tma_load_2d(&tm_b, &full[s], a + kABytes, (seg == 1 ? dh : 0) + kx, t * kTN);
         }
       }
       if (!ok) atomicOr(err, kDevErrSpin);
@@ -201,7 +212,7 @@ __global__ void __launch_bounds__(kExactThreads, 1)
           break;
         }
         tc_fence_after();
-        for (int kc = 0; kc < kchunks; ++kc, ++it) {
+        for (int kc = 0; kc < 3 * kchunks; ++kc, ++it) {
           const uint32_t s = it % kStages, use = it / kStages;
           if (!mbar_wait(&full[s], use & 1)) {
             ok = false;
@@ -264,72 +275,210 @@ __global__ void __launch_bounds__(kExactThreads, 1)
   }
 }
 
-// Rigorous bound on |approx - canonical| for one pair: BF16 rounding of both
-// operands (2u + u^2 with u = 2^-9) plus FP32 accumulation of <= 2048 terms in
-// the tensor core and in the canonical chain, times 2 (the distance carries
-// -2 dot), applied to sum|a_i b_i| <= |a||b|; plus the rounding of the norm
-// sums.  0.009 covers 2 * (0.0039101 + 2048 * 2^-23 + 2048 * 2^-24) = 0.00855.
-GM_D float pair_bound(float na, float nb) {
-  return __fadd_rn(__fmul_rn(0.009f, __fsqrt_ru(__fmul_ru(na, nb))),
-                   __fadd_rn(__fmul_rn(1e-6f, __fadd_rn(na, nb)), 1e-30f));
+// Rigorous bound on |approx - canonical| for one pair, as coef * sqrt(na nb)
+// + 2^-21 (na + nb), with coef from exact_bound_coef.  Both distances share
+// fl(na + nb); they differ by 2 |v - dot_c| plus the final subtraction's
+// rounding (2^-24 of |s - 2v| and of |s - 2 dot_c|, each below 2 (na + nb)
+// for any pair within the bound).
+GM_D float pair_bound(float coef, float na, float nb) {
+  return __fadd_ru(__fmul_ru(coef, __fsqrt_ru(__fmul_ru(na, nb))),
+                   __fadd_ru(__fmul_ru(4.8e-7f, __fadd_ru(na, nb)), 1e-30f));
 }
 
-GM_D float canon_pair(const float *X, int ld, int d, const float *norms, int a, int b) {
-  const float *xa = X + (size_t)a * ld;
-  const float *xb = X + (size_t)b * ld;
+// ---- screen: bound test, exact FP32 re-score, exact top-32 -----------------
+//
+// Per block of batch rows (brow0 .. brow0 + nrows) against columns [0, n):
+//  k_row_scan    CTA per batch row: threshold T (32nd smallest upper bound),
+//                candidate columns whose lower bound reaches T
+//  k_col_scan    thread per existing row j < n_exist: batch rows whose lower
+//                bound reaches j's current 32nd distance, as a contiguous
+//                segment of the column pool
+//  k_row_dists   canonical distances of the row candidates
+//  k_pair_dists  canonical distances of the column pool
+//  k_row_select  warp per batch row: exact top-32 keys of its candidates
+//  k_col_merge   thread per existing row: merges its segment into its list
+// Both merges are order independent: a list ends as the 32 smallest keys of
+// its old entries and every candidate, and keys are unique (distinct ids).
+//
+// Canonical distances are sequential FP32 fused multiply-add chains over the
+// features; a warp forms 32 chains at once, one per lane, from feature rows
+// staged 32 columns at a time in shared memory by coalesced loads (lane l
+// reads tile row l at column i: bank (l * 33 + i) mod 32, conflict free).
+// fmaf(a, b, c) = fmaf(b, a, c) exactly, so d(x, y) = d(y, x) bit for bit.
+
+constexpr int kScanThreads = 256;
+constexpr int kTile = 32;
+constexpr int kTileLd = 33;
+
+GM_D unsigned block_sum(unsigned v, unsigned *red) {
+  v = __reduce_add_sync(0xffffffffu, v);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  unsigned t = 0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += red[i];
+  return t;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    k_row_scan(const float *D, long ldD, int brow0, int n, const float *norms, float coef,
+               int *cand, long cand_ld, int *row_cnt, unsigned long long *stat) {
+  __shared__ unsigned red[kScanThreads / 32];
+  __shared__ int s_cnt;
+  const int ml = blockIdx.x, row = brow0 + ml, tid = threadIdx.x, lane = tid & 31;
+  const float nm = norms[row];
+  const float *Dr = D + (long)ml * ldD;
+  const float inf = __int_as_float(0x7f800000);
+  float u0 = inf, u1 = inf, u2 = inf, u3 = inf;  // this thread's 4 smallest upper bounds
+  for (int j = tid; j < n; j += kScanThreads) {
+    if (j == row) continue;
+    const float x = fmaxf(__fadd_ru(Dr[j], pair_bound(coef, nm, norms[j])), 0.0f);
+    if (x < u3) {
+      u3 = x;
+      if (u3 < u2) { const float t = u2; u2 = u3; u3 = t; }
+      if (u2 < u1) { const float t = u1; u1 = u2; u2 = t; }
+      if (u1 < u0) { const float t = u0; u0 = u1; u1 = t; }
+    }
+  }
+  // T = 32nd smallest of the block's values: at least 32 distinct columns have
+  // upper bounds (so canonical distances) at or below it.  Nonnegative floats
+  // order as their bit patterns: binary-search the smallest such pattern.
+  unsigned lo = 0u, hi = 0x7f800000u;
+  const unsigned b0 = __float_as_uint(u0), b1 = __float_as_uint(u1), b2 = __float_as_uint(u2),
+                 b3 = __float_as_uint(u3);
+  while (lo < hi) {
+    const unsigned mid = lo + ((hi - lo) >> 1);
+    const unsigned c = (unsigned)(b0 <= mid) + (unsigned)(b1 <= mid) + (unsigned)(b2 <= mid) +
+                       (unsigned)(b3 <= mid);
+    if (block_sum(c, red) >= 32u) hi = mid;
+    else lo = mid + 1u;
+  }
+  const float T = n - 1 < 32 ? inf : __uint_as_float(hi);  // fewer than 32 others: all
+  if (tid == 0) s_cnt = 0;
+  __syncthreads();
+  int *cl = cand + (long)ml * cand_ld;
+  for (int j0 = 0; j0 < n; j0 += kScanThreads) {
+    const int j = j0 + tid;
+    const bool keep = j < n && j != row && __fsub_rd(Dr[j], pair_bound(coef, nm, norms[j])) <= T;
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    int base = 0;
+    if (lane == 0 && bal) base = atomicAdd(&s_cnt, __popc(bal));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (keep) cl[base + __popc(bal & ((1u << lane) - 1u))] = j;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    row_cnt[ml] = s_cnt;
+    if (stat) {
+      atomicAdd(&stat[5], (unsigned long long)n);
+      atomicAdd(&stat[6], (unsigned long long)s_cnt);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    k_col_scan(const float *D, long ldD, int n_exist, int brow0, int nrows, const float *norms,
+               float coef, const Key *g_key, int *pool_j, int *pool_m, long pool_cap, int *seg,
+               int *counter, unsigned *err, unsigned long long *stat) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_exist) return;
+  const float w = key_dist(g_key[(size_t)j * kListW + kListW - 1]);
+  const float nj = norms[j];
+  int cnt = 0;
+  for (int ml = 0; ml < nrows; ++ml)
+    cnt += __fsub_rd(D[(long)ml * ldD + j], pair_bound(coef, nj, norms[brow0 + ml])) <= w;
+  int base = 0;
+  if (cnt) {
+    base = atomicAdd(counter, cnt);
+    if ((long)base + cnt > pool_cap) {
+      atomicOr(err, kDevErrOverflow);
+      cnt = 0;
+    } else {
+      int q = base;
+      for (int ml = 0; ml < nrows && q < base + cnt; ++ml) {
+        if (__fsub_rd(D[(long)ml * ldD + j], pair_bound(coef, nj, norms[brow0 + ml])) <= w) {
+          pool_j[q] = j;
+          pool_m[q] = ml;
+          ++q;
+        }
+      }
+      if (stat) atomicAdd(&stat[6], (unsigned long long)cnt);
+    }
+  }
+  seg[2 * j] = base;
+  seg[2 * j + 1] = cnt;
+}
+
+// Stages rows ra / rb (this lane's pair; dummies for idle lanes) 32 features
+// at a time and runs each lane's canonical chain.
+GM_D float warp_pair_dot(const float *X, int ld, int d, int ra, int rb,
+                         float (*ta)[kTileLd], float (*tb)[kTileLd]) {
+  const int lane = threadIdx.x & 31;
   float dot = 0.0f;
-  for (int i = 0; i < d; ++i) dot = __fmaf_rn(xa[i], xb[i], dot);
-  return canon_dist(norms[a], norms[b], dot);
+  for (int i0 = 0; i0 < d; i0 += kTile) {
+    const int c = i0 + lane;
+#pragma unroll 8
+    for (int r = 0; r < kTile; ++r) {
+      const int a = __shfl_sync(0xffffffffu, ra, r);
+      const int b = __shfl_sync(0xffffffffu, rb, r);
+      ta[r][lane] = c < d ? X[(size_t)a * ld + c] : 0.0f;
+      tb[r][lane] = c < d ? X[(size_t)b * ld + c] : 0.0f;
+    }
+    __syncwarp();
+    const int lim = min(kTile, d - i0);
+    for (int i = 0; i < lim; ++i) dot = __fmaf_rn(ta[lane][i], tb[lane][i], dot);
+    __syncwarp();
+  }
+  return dot;
 }
 
-// One warp per batch row: an upper bound T on its 32nd smallest distance (the
-// largest of the 32 per-lane minima of the upper bounds: there are 32 distinct
-// columns at or below it), every column whose lower bound reaches T, exact
-// re-scoring of those, and the exact top-32 keys written as the row's list.
+constexpr int kPairWarps = 4;
+__global__ void __launch_bounds__(kPairWarps * 32)
+    k_pair_dists(const float *X, int ld, int d, const float *norms, int brow0, const int *pool_j,
+                 const int *pool_m, float *pool_d, const int *counter, long pool_cap) {
+  __shared__ float ta[kPairWarps][kTile][kTileLd], tb[kPairWarps][kTile][kTileLd];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long total = min((long)*counter, pool_cap);
+  const long nw = (long)gridDim.x * kPairWarps;
+  for (long g = ((long)blockIdx.x * kPairWarps + w) * 32; g < total; g += nw * 32) {
+    const long e = g + lane;
+    const bool ok = e < total;
+    const int a = ok ? pool_j[e] : 0;
+    const int b = ok ? brow0 + pool_m[e] : 0;
+    const float dot = warp_pair_dot(X, ld, d, a, b, ta[w], tb[w]);
+    if (ok) pool_d[e] = canon_dist(norms[a], norms[b], dot);
+  }
+}
+
+__global__ void __launch_bounds__(kPairWarps * 32)
+    k_row_dists(const float *X, int ld, int d, const float *norms, int brow0, const int *cand,
+                long cand_ld, const int *row_cnt, float *cand_d) {
+  __shared__ float ta[kPairWarps][kTile][kTileLd], tb[kPairWarps][kTile][kTileLd];
+  const int ml = blockIdx.x, row = brow0 + ml;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cnt = row_cnt[ml];
+  const int *cl = cand + (long)ml * cand_ld;
+  for (int g = w * 32; g < cnt; g += kPairWarps * 32) {
+    const int c = g + lane;
+    const int b = c < cnt ? cl[c] : row;
+    const float dot = warp_pair_dot(X, ld, d, row, b, ta[w], tb[w]);
+    if (c < cnt) cand_d[(long)ml * cand_ld + c] = canon_dist(norms[row], norms[b], dot);
+  }
+}
+
 constexpr int kRowWarps = 4;
-__global__ void k_exact_rows(const float *D, long ldD, int arow0, int mrow0, int nrows, int n,
-                             const float *X, int ld, int d, const float *norms, Key *g_key,
-                             int *cand, long cand_ld, unsigned long long *stat) {
+__global__ void k_row_select(const float *cand_d, int brow0, int nrows, const int *cand,
+                             long cand_ld, const int *row_cnt, Key *g_key) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ml = blockIdx.x * kRowWarps + warp;
   if (ml >= nrows) return;
-  const int m = mrow0 + ml;       // batch-local row
-  const int row = arow0 + m;      // global row
-  const float nm = norms[row];
-  const float *Dr = D + (long)m * ldD;
-  float lmin = __int_as_float(0x7f800000);
-  for (int j = lane; j < n; j += 32) {
-    if (j == row) continue;
-    lmin = fminf(lmin, __fadd_ru(Dr[j], pair_bound(nm, norms[j])));
-  }
-  float T = lmin;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) T = fmaxf(T, __shfl_xor_sync(0xffffffffu, T, o));
-  // fewer than 32 other columns: take them all
-  if (n - 1 < 32) T = __int_as_float(0x7f800000);
-  int *cl = cand + (long)ml * cand_ld;
-  int cnt = 0;
-  for (int j0 = 0; j0 < n; j0 += 32) {
-    const int j = j0 + lane;
-    bool keep = false;
-    if (j < n && j != row) keep = __fsub_rd(Dr[j], pair_bound(nm, norms[j])) <= T;
-    const unsigned bal = __ballot_sync(0xffffffffu, keep);
-    if (keep) cl[cnt + __popc(bal & ((1u << lane) - 1u))] = j;
-    cnt += __popc(bal);
-  }
-  __syncwarp();
-  if (lane == 0 && stat) {
-    atomicAdd(&stat[5], (unsigned long long)n);
-    atomicAdd(&stat[6], (unsigned long long)cnt);
-  }
+  const int cnt = row_cnt[ml];
+  const int *cl = cand + (long)ml * cand_ld;
+  const float *dr = cand_d + (long)ml * cand_ld;
   Key mine = kEmptyKey;
   for (int c0 = 0; c0 < cnt; c0 += 32) {
     const int c = c0 + lane;
-    Key ck = ~(Key)0;
-    if (c < cnt) {
-      const int j = cl[c];
-      ck = make_key(canon_pair(X, ld, d, norms, row, j), j);
-    }
+    const Key ck = c < cnt ? make_key(dr[c], cl[c]) : ~(Key)0;
     // insert the (up to) 32 new keys one at a time into the sorted warp list
     for (int src = 0; src < 32 && c0 + src < cnt; ++src) {
       const Key k = __shfl_sync(0xffffffffu, ck, src);
@@ -341,29 +490,20 @@ __global__ void k_exact_rows(const float *D, long ldD, int arow0, int mrow0, int
       else if (lane == pos) mine = k;
     }
   }
-  g_key[(size_t)row * kListW + lane] = mine;
+  g_key[(size_t)(brow0 + ml) * kListW + lane] = mine;
 }
 
-// One thread per existing row j < n_exist: batch rows of this block whose lower
-// bound does not exceed j's current last entry are re-scored and merged into
-// j's list (the thread owns the list; batch rows in ascending order).
-__global__ void k_exact_cols(const float *D, long ldD, int n_exist, int brow0, int nrows,
-                             const float *X, int ld, int d, const float *norms, Key *g_key,
-                             int *dirty, unsigned long long *stat) {
+__global__ void k_col_merge(int n_exist, int brow0, const int *seg, const int *pool_m,
+                            const float *pool_d, Key *g_key, int *dirty) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n_exist) return;
+  const int base = seg[2 * j], cnt = seg[2 * j + 1];
+  if (!cnt) return;
   Key *lst = g_key + (size_t)j * kListW;
   Key worst = lst[kListW - 1];
-  const float nj = norms[j];
   bool changed = false;
-  unsigned rescored = 0;
-  for (int ml = 0; ml < nrows; ++ml) {
-    const float a = D[(long)ml * ldD + j];
-    const int row = brow0 + ml;
-    const float wd = key_dist(worst);
-    if (__fsub_rd(a, pair_bound(nj, norms[row])) > wd) continue;
-    const Key ck = make_key(canon_pair(X, ld, d, norms, j, row), row);
-    ++rescored;
+  for (int q = base; q < base + cnt; ++q) {
+    const Key ck = make_key(pool_d[q], brow0 + pool_m[q]);
     if (!(ck < worst)) continue;
     int pos = kListW - 1;
     while (pos > 0 && ck < lst[pos - 1]) {
@@ -375,7 +515,6 @@ __global__ void k_exact_cols(const float *D, long ldD, int n_exist, int brow0, i
     changed = true;
   }
   if (changed) dirty[j] = 1;
-  if (stat && rescored) atomicAdd(&stat[6], (unsigned long long)rescored);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
@@ -398,11 +537,35 @@ inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
 int exact_dh(int d) { return (d + kTK - 1) / kTK * kTK; }
 
+// coef of pair_bound for d features (dh padded).  With S = sum |a_i b_i| <=
+// |a||b| (Cauchy-Schwarz) and u = 2^-8 the BF16 unit roundoff:
+//  * operands: a_i b_i - (hi hi + hi lo + lo hi) = lo lo + hi r + lo r + r hi + ...
+//    with |lo| <= u|a_i|, |r| = |a_i - hi - lo| <= u^2 |a_i|: below 3.1 u^2 S;
+//  * tensor-core accumulation of m = 3 dh exact products: every operand of
+//    every internal addition (the products, and the running sum once per
+//    K=16 instruction; m/4 allows for up to four internal stages each) is cut
+//    by at most 2^-23 of the largest magnitude involved, itself at most the
+//    products' magnitude sum (1 + u)^2 S + 2 u (1 + u) S < 1.02 S: below
+//    (1.25 m + 1) 2^-23 * 1.02 S;
+//  * canonical FP32 chain of d fused multiply-adds (round to nearest):
+//    below d 2^-24 S (1 + d 2^-24);
+//  times 2 for -2 dot, and 1 + d 2^-23 because sqrt(na nb) is formed from FP32
+//  norms that may fall short of |a|^2 |b|^2 by that factor.
+float exact_bound_coef(int d, int dh) {
+  const double u = std::ldexp(1.0, -8);
+  const double m = 3.0 * dh;
+  const double op = 3.1 * u * u;
+  const double acc = (1.25 * m + 1.0) * std::ldexp(1.0, -23) * 1.02;
+  const double canon = d * std::ldexp(1.0, -24) * (1.0 + d * std::ldexp(1.0, -24));
+  const double c = 2.0 * (op + acc + canon) * (1.0 + d * std::ldexp(1.0, -23)) * 1.001;
+  return (float)(c * (1.0 + 1e-6));
+}
+
 bool make_row_maps(void *xh, int n_cap, int dh, ExactMaps *out) {
   auto enc = get_encode();
   if (!enc) return false;
-  const cuuint64_t dims[2] = {(cuuint64_t)dh, (cuuint64_t)std::max(n_cap, 1)};
-  const cuuint64_t strides[1] = {(cuuint64_t)dh * 2};
+  const cuuint64_t dims[2] = {(cuuint64_t)dh * 2, (cuuint64_t)std::max(n_cap, 1)};
+  const cuuint64_t strides[1] = {(cuuint64_t)dh * 4};
   const cuuint32_t estr[2] = {1, 1};
   const cuuint32_t box_a[2] = {(cuuint32_t)kTK, (cuuint32_t)kTM};
   const cuuint32_t box_b[2] = {(cuuint32_t)kTK, (cuuint32_t)kTN};
@@ -443,20 +606,37 @@ void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int ro
   memcpy(&ta, maps.a, sizeof(ta));
   memcpy(&tb, maps.b, sizeof(tb));
   k_exact_dist<<<dim3(gx, m_tiles), kExactThreads, kExactSmem, s>>>(
-      ta, tb, row0 + blk0, nrows, n, dh / kTK, st.norms, D, ldD, st.err);
+      ta, tb, row0 + blk0, nrows, n, dh / kTK, dh, st.norms, D, ldD, st.err);
   note_launch();
 }
 
 void launch_exact_screen(const DevState &st, int row0, int blk0, int nrows, int n,
-                         const float *D, long ldD, int *cand, long cand_ld, cudaStream_t s) {
+                         const ExactScreen &x, long ldD, int sms, cudaStream_t s) {
   if (nrows <= 0 || n <= 0) return;
   const int brow0 = row0 + blk0;  // global first row of the block
-  k_exact_rows<<<cdiv(nrows, kRowWarps), kRowWarps * 32, 0, s>>>(
-      D, ldD, brow0, 0, nrows, n, st.X, st.ld, st.d, st.norms, st.g_key, cand, cand_ld, st.stat);
+  const float coef = exact_bound_coef(st.d, exact_dh(st.d));
+  k_row_scan<<<nrows, kScanThreads, 0, s>>>(x.D, ldD, brow0, n, st.norms, coef, x.cand, ldD,
+                                            x.row_cnt, st.stat);
   note_launch();
   if (row0 > 0) {
-    k_exact_cols<<<cdiv(row0, 128), 128, 0, s>>>(D, ldD, row0, brow0, nrows, st.X, st.ld, st.d,
-                                                 st.norms, st.g_key, st.dirty, st.stat);
+    cudaMemsetAsync(x.counter, 0, sizeof(int), s);
+    k_col_scan<<<cdiv(row0, kScanThreads), kScanThreads, 0, s>>>(
+        x.D, ldD, row0, brow0, nrows, st.norms, coef, st.g_key, x.pool_j, x.pool_m, x.pool_cap,
+        x.seg, x.counter, st.err, st.stat);
+    note_launch();
+  }
+  k_row_dists<<<nrows, kPairWarps * 32, 0, s>>>(st.X, st.ld, st.d, st.norms, brow0, x.cand, ldD,
+                                               x.row_cnt, x.cand_d);
+  note_launch();
+  k_row_select<<<cdiv(nrows, kRowWarps), kRowWarps * 32, 0, s>>>(x.cand_d, brow0, nrows, x.cand,
+                                                                 ldD, x.row_cnt, st.g_key);
+  note_launch();
+  if (row0 > 0) {
+    k_pair_dists<<<4 * std::max(sms, 1), kPairWarps * 32, 0, s>>>(
+        st.X, st.ld, st.d, st.norms, brow0, x.pool_j, x.pool_m, x.pool_d, x.counter, x.pool_cap);
+    note_launch();
+    k_col_merge<<<cdiv(row0, kScanThreads), kScanThreads, 0, s>>>(row0, brow0, x.seg, x.pool_m,
+                                                                  x.pool_d, st.g_key, st.dirty);
     note_launch();
   }
 }

@@ -107,10 +107,22 @@ void launch_to_bf16(const DevState &st, void *xh, int dh, int row0, int nrows, c
 // against rows [0, n) on the tensor cores.
 void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
                        int nrows, int n, float *D, long ldD, int sms, cudaStream_t s);
+// Screen scratch of one block of batch rows (capacity rows x n_cap each).
+struct ExactScreen {
+  float *D = nullptr;     // rows x ldD approximate distances
+  int *cand = nullptr;    // rows x ldD candidate columns per batch row
+  float *cand_d = nullptr;  // rows x ldD their canonical distances
+  int *row_cnt = nullptr; // rows candidate counts
+  int *pool_j = nullptr, *pool_m = nullptr;  // column-direction pairs
+  float *pool_d = nullptr;
+  int *seg = nullptr;     // n_cap x 2: (first pair, pairs) per existing row
+  int *counter = nullptr; // pairs in the pool
+  long pool_cap = 0;
+};
 // Exact lists of those rows (bound, FP32 re-score, top-32) and their offers to
-// rows [0, row0).  cand: nrows x cand_ld scratch.
+// rows [0, row0).
 void launch_exact_screen(const DevState &st, int row0, int blk0, int nrows, int n,
-                         const float *D, long ldD, int *cand, long cand_ld, cudaStream_t s);
+                         const ExactScreen &x, long ldD, int sms, cudaStream_t s);
 
 // ---- update (gm_kernels_update.cu) ----
 void launch_sample_graph(const DevState &st, const UpdScratch &u,

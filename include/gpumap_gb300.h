@@ -96,7 +96,7 @@ typedef struct gm_stats {
   uint64_t sgd_negatives;     /* negative samples drawn */
   uint64_t exact_launches;    /* tensor-core distance launches (precision 1) */
   double exact_ms;            /* their summed time */
-  double exact_flops;         /* 2 x rows x columns x padded features, summed */
+  double exact_flops;         /* 6 x rows x columns x padded features (split BF16), summed */
   double screen_ms;           /* bound + FP32 re-score + top-32 kernels */
   uint64_t exact_pairs;       /* batch x column pairs formed on the tensor cores */
   uint64_t exact_rescored;    /* pairs re-scored in FP32 */

@@ -368,14 +368,24 @@ int gm_op_sgd(float *emb, int64_t n, const int32_t *head, const int32_t *tail,
     cudaMemcpyAsync(sc, iscal, 64, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync((char *)sc + 64, fscal, 64, cudaMemcpyHostToDevice, s);
     gm::launch_epoch_init(eps, (int)nnz, neg_rate, (float *)ns, (float *)nn, s);
-    gm::launch_sgd(emb, head, tail, eps, (float *)ns, (float *)nn, (const int *)sc,
-                   (const float *)((char *)sc + 64), (int)((nnz + 255) / 256), alpha0, gamma, a,
-                   b, n_epochs, neg_rate, seed, s);
-    const cudaError_t err = cudaStreamSynchronize(s);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    // scalars: iscal[0..16) at sc, fscal at sc + 64; grid-barrier words in
+    // iscal[8..9], device error word in iscal[10]
+    int *isc = (int *)sc;
+    const cudaError_t le = gm::launch_sgd_persistent(
+        emb, head, tail, eps, (float *)ns, (float *)nn, isc, (const float *)((char *)sc + 64),
+        alpha0, gamma, a, b, n_epochs, neg_rate, seed, (unsigned *)(isc + gm::kIscalBarrier),
+        (unsigned *)(isc + 10), dev, s);
+    unsigned dev_err = 0;
+    if (le == cudaSuccess) cudaMemcpyAsync(&dev_err, isc + 10, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    const cudaError_t err = le != cudaSuccess ? le : cudaStreamSynchronize(s);
+    if (le != cudaSuccess) cudaGetLastError();
     cudaFree(ns);
     cudaFree(nn);
     cudaFree(sc);
     if (err != cudaSuccess) throw gm::Error(GM_ERR_CUDA, cudaGetErrorString(err));
+    if (dev_err) throw gm::Error(GM_ERR_DEVICE, "SGD grid barrier wait ran out");
   });
 }
 

@@ -110,14 +110,28 @@ GM_D float gm_expf(float x) {
   p = __fmaf_rn(p, r, 0.5f);
   p = __fmaf_rn(p, r, 1.0f);
   p = __fmaf_rn(p, r, 1.0f);
-  return ldexpf(p, (int)n);
+  // p * 2^n: exponent-field add when the result stays normal (exact, the
+  // same value ldexpf gives), ldexpf otherwise
+  const int ni = (int)n;
+  const unsigned pb = __float_as_uint(p);
+  const int ef = (int)((pb >> 23) & 0xffu) + ni;
+  if (ef >= 1 && ef <= 254) return __uint_as_float(pb + ((unsigned)ni << 23));
+  return ldexpf(p, ni);
 }
 
 GM_D float gm_logf(float x) {
   if (!(x > 0.0f)) return (x == 0.0f) ? __int_as_float(0xff800000) : __int_as_float(0x7fc00000);
   if (x == __int_as_float(0x7f800000)) return x;
-  int e;
-  float m = frexpf(x, &e);
+  // frexpf by bit fields: x = m * 2^e, m in [0.5, 1) (subnormals scaled by
+  // 2^23 first, exactly)
+  unsigned u = __float_as_uint(x);
+  int e = 0;
+  if (u < 0x00800000u) {
+    u = __float_as_uint(__fmul_rn(x, 8388608.0f));
+    e = -23;
+  }
+  e += (int)(u >> 23) - 126;
+  float m = __uint_as_float((u & 0x007fffffu) | 0x3f000000u);
   if (m < 0.70710678f) {
     m = __fmul_rn(m, 2.0f);
     e -= 1;

@@ -78,6 +78,7 @@ Session::Session(const gm_params &p) : p_(p) {
   try {
     st_.X = (float *)dalloc(Nm * st_.ld * sizeof(float));
     st_.norms = (float *)dalloc(Nm * sizeof(float));
+    st_.snorms = (float *)dalloc(Nm * sizeof(float));
     st_.g_key = (unsigned long long *)dalloc(Nm * kListW * sizeof(unsigned long long));
     st_.locks = (int *)dalloc(Nm * sizeof(int));
     st_.dirty = (int *)dalloc(Nm * sizeof(int));
@@ -158,6 +159,7 @@ Session::Session(const gm_params &p) : p_(p) {
   cudaStream_t s = stream_;
   ck(cudaMemsetAsync(st_.X, 0, Nm * st_.ld * sizeof(float), s), "memset");
   ck(cudaMemsetAsync(st_.norms, 0, Nm * sizeof(float), s), "memset");
+  ck(cudaMemsetAsync(st_.snorms, 0, Nm * sizeof(float), s), "memset");
   fill_u64(st_.g_key, kEmptyKey, Nm * kListW, s);
   ck(cudaMemsetAsync(st_.locks, 0, Nm * sizeof(int), s), "memset");
   ck(cudaMemsetAsync(st_.dirty, 0, Nm * sizeof(int), s), "memset");
@@ -195,7 +197,6 @@ Session::Session(const gm_params &p) : p_(p) {
 
 Session::~Session() {
   if (stream_) cudaStreamSynchronize(stream_);
-  if (sgd_exec_) cudaGraphExecDestroy(sgd_exec_);
   for (auto &e : ev_pool_) cudaEventDestroy(e);
   for (auto &pr : ev_pending_) {
     cudaEventDestroy(pr.a);
@@ -641,7 +642,7 @@ uint32_t Session::embed(uint32_t n_ops) {
   launch_schedule(ni, nb, k, p_.alpha, (int)p_.max_epoch, (int)p_.negative_sample_rate, es_, s);
   launch_set_int(es_.iscal + kIscalN, ni, s);
   timed_begin(2);
-  run_sgd_graph();
+  run_sgd();
   timed_end(2);
   const int nu = ni - nb;
   if (nu > 0) {
@@ -653,35 +654,16 @@ uint32_t Session::embed(uint32_t n_ops) {
   return (uint32_t)nb;
 }
 
-// The max_epoch SGD launches of one embedding call, captured once as a CUDA
-// graph and replayed: every parameter is fixed for the session (sizes are read
-// from device scalars), so only a reallocation of the edge buffers forces a
-// new capture.
-void Session::run_sgd_graph() {
+// The max_epoch SGD epochs of one embedding call: one cooperative launch
+// with a grid barrier between epochs (sizes are read from device scalars).
+void Session::run_sgd() {
   if (p_.max_epoch == 0) return;
-  if (sgd_grid_ == 0) {
-    int sms = 0;
-    ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_), "attr");
-    sgd_grid_ = 4 * std::max(sms, 1);
-  }
-  bool fresh = false;
-  if (!sgd_exec_ || sgd_key_ != (const void *)es_.t_row) {
-    if (sgd_exec_) cudaGraphExecDestroy(sgd_exec_);
-    sgd_exec_ = nullptr;
-    cudaGraph_t g = nullptr;
-    ck(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "capture begin");
-    launch_sgd(st_.emb, es_.t_row, es_.flag_tail, es_.t_val, es_.next_s, es_.next_n, es_.iscal,
-               es_.fscal, sgd_grid_, p_.alpha, 1.0f, p_.a, p_.b, (int)p_.max_epoch,
-               (int)p_.negative_sample_rate, 42ull, stream_, st_.stat);
-    ck(cudaStreamEndCapture(stream_, &g), "capture end");
-    const cudaError_t e = cudaGraphInstantiate(&sgd_exec_, g, 0);
-    cudaGraphDestroy(g);
-    ck(e, "graph instantiate");
-    sgd_key_ = (const void *)es_.t_row;
-    fresh = true;
-  }
-  ck(cudaGraphLaunch(sgd_exec_, stream_), "graph launch");
-  if (!fresh) note_launch((int)p_.max_epoch);
+  ck(launch_sgd_persistent(st_.emb, es_.t_row, es_.flag_tail, es_.t_val, es_.next_s, es_.next_n,
+                           es_.iscal, es_.fscal, p_.alpha, 1.0f, p_.a, p_.b, (int)p_.max_epoch,
+                           (int)p_.negative_sample_rate, 42ull,
+                           (unsigned *)(es_.iscal + kIscalBarrier), st_.err, device_, stream_,
+                           st_.stat),
+     "SGD launch");
 }
 
 void Session::close() {

@@ -93,7 +93,7 @@ class Session {
   void timed_begin(int slot);
   void timed_end(int slot);
   void collect_timings();
-  void run_sgd_graph();
+  void run_sgd();
 
   gm_params p_;
   int device_ = 0;
@@ -143,11 +143,6 @@ class Session {
   int ex_block_ = 0;
   ExactScreen xs_{};
   int sms_ = 0;
-
-  // captured SGD epochs
-  cudaGraphExec_t sgd_exec_ = nullptr;
-  const void *sgd_key_ = nullptr;
-  int sgd_grid_ = 0;
 };
 
 }  // namespace gm

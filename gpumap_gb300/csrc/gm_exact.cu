@@ -279,9 +279,10 @@ __global__ void __launch_bounds__(kExactThreads, 1)
 // + 2^-21 (na + nb), with coef from exact_bound_coef.  Both distances share
 // fl(na + nb); they differ by 2 |v - dot_c| plus the final subtraction's
 // rounding (2^-24 of |s - 2v| and of |s - 2 dot_c|, each below 2 (na + nb)
-// for any pair within the bound).
-GM_D float pair_bound(float coef, float na, float nb) {
-  return __fadd_ru(__fmul_ru(coef, __fsqrt_ru(__fmul_ru(na, nb))),
+// for any pair within the bound).  sa, sb: sqrt(na), sqrt(nb) rounded up, so
+// sa * sb (rounded up) >= sqrt(na nb).
+GM_D float pair_bound(float coef, float sa, float sb, float na, float nb) {
+  return __fadd_ru(__fmul_ru(coef, __fmul_ru(sa, sb)),
                    __fadd_ru(__fmul_ru(4.8e-7f, __fadd_ru(na, nb)), 1e-30f));
 }
 
@@ -321,18 +322,20 @@ GM_D unsigned block_sum(unsigned v, unsigned *red) {
 }
 
 __global__ void __launch_bounds__(kScanThreads)
-    k_row_scan(const float *D, long ldD, int brow0, int n, const float *norms, float coef,
-               int *cand, long cand_ld, int *row_cnt, unsigned long long *stat) {
+    k_row_scan(const float *D, long ldD, int brow0, int n, const float *norms,
+               const float *snorms, float coef, int *cand, long cand_ld, int *row_cnt,
+               unsigned long long *stat) {
   __shared__ unsigned red[kScanThreads / 32];
   __shared__ int s_cnt;
   const int ml = blockIdx.x, row = brow0 + ml, tid = threadIdx.x, lane = tid & 31;
-  const float nm = norms[row];
+  const float nm = norms[row], sm = snorms[row];
   const float *Dr = D + (long)ml * ldD;
   const float inf = __int_as_float(0x7f800000);
   float u0 = inf, u1 = inf, u2 = inf, u3 = inf;  // this thread's 4 smallest upper bounds
   for (int j = tid; j < n; j += kScanThreads) {
     if (j == row) continue;
-    const float x = fmaxf(__fadd_ru(Dr[j], pair_bound(coef, nm, norms[j])), 0.0f);
+    const float x =
+        fmaxf(__fadd_ru(Dr[j], pair_bound(coef, sm, snorms[j], nm, norms[j])), 0.0f);
     if (x < u3) {
       u3 = x;
       if (u3 < u2) { const float t = u2; u2 = u3; u3 = t; }
@@ -359,7 +362,8 @@ __global__ void __launch_bounds__(kScanThreads)
   int *cl = cand + (long)ml * cand_ld;
   for (int j0 = 0; j0 < n; j0 += kScanThreads) {
     const int j = j0 + tid;
-    const bool keep = j < n && j != row && __fsub_rd(Dr[j], pair_bound(coef, nm, norms[j])) <= T;
+    const bool keep = j < n && j != row &&
+                      __fsub_rd(Dr[j], pair_bound(coef, sm, snorms[j], nm, norms[j])) <= T;
     const unsigned bal = __ballot_sync(0xffffffffu, keep);
     int base = 0;
     if (lane == 0 && bal) base = atomicAdd(&s_cnt, __popc(bal));
@@ -376,17 +380,33 @@ __global__ void __launch_bounds__(kScanThreads)
   }
 }
 
+constexpr int kColRows = 1024;  // batch rows whose norms a col-scan CTA caches
 __global__ void __launch_bounds__(kScanThreads)
     k_col_scan(const float *D, long ldD, int n_exist, int brow0, int nrows, const float *norms,
-               float coef, const Key *g_key, int *pool_j, int *pool_m, long pool_cap, int *seg,
-               int *counter, unsigned *err, unsigned long long *stat) {
+               const float *snorms, float coef, const Key *g_key, int *pool_j, int *pool_m,
+               long pool_cap, int *seg, int *counter, unsigned *err, unsigned long long *stat) {
+  __shared__ float s_n[kColRows], s_s[kColRows];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n_exist) return;
-  const float w = key_dist(g_key[(size_t)j * kListW + kListW - 1]);
-  const float nj = norms[j];
+  const bool live = j < n_exist;
+  const float w = live ? key_dist(g_key[(size_t)j * kListW + kListW - 1]) : 0.0f;
+  const float nj = live ? norms[j] : 0.0f, sj = live ? snorms[j] : 0.0f;
   int cnt = 0;
-  for (int ml = 0; ml < nrows; ++ml)
-    cnt += __fsub_rd(D[(long)ml * ldD + j], pair_bound(coef, nj, norms[brow0 + ml])) <= w;
+  for (int m0 = 0; m0 < nrows; m0 += kColRows) {
+    const int mr = min(kColRows, nrows - m0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < mr; i += blockDim.x) {
+      s_n[i] = norms[brow0 + m0 + i];
+      s_s[i] = snorms[brow0 + m0 + i];
+    }
+    __syncthreads();
+    if (live) {
+      const float *Dc = D + (long)m0 * ldD + j;
+#pragma unroll 8
+      for (int i = 0; i < mr; ++i)
+        cnt += __fsub_rd(Dc[(long)i * ldD], pair_bound(coef, sj, s_s[i], nj, s_n[i])) <= w;
+    }
+  }
+  if (!live) return;
   int base = 0;
   if (cnt) {
     base = atomicAdd(counter, cnt);
@@ -394,9 +414,11 @@ __global__ void __launch_bounds__(kScanThreads)
       atomicOr(err, kDevErrOverflow);
       cnt = 0;
     } else {
+      // second pass (rare hits): same test, norms from global memory
       int q = base;
       for (int ml = 0; ml < nrows && q < base + cnt; ++ml) {
-        if (__fsub_rd(D[(long)ml * ldD + j], pair_bound(coef, nj, norms[brow0 + ml])) <= w) {
+        if (__fsub_rd(D[(long)ml * ldD + j],
+                      pair_bound(coef, sj, snorms[brow0 + ml], nj, norms[brow0 + ml])) <= w) {
           pool_j[q] = j;
           pool_m[q] = ml;
           ++q;
@@ -493,28 +515,37 @@ __global__ void k_row_select(const float *cand_d, int brow0, int nrows, const in
   g_key[(size_t)(brow0 + ml) * kListW + lane] = mine;
 }
 
+// Warp per existing row j with pairs: lane l holds entry l of j's sorted list;
+// each new key is inserted by a ballot on the lanes whose entry it precedes.
+constexpr int kMergeWarps = 8;
 __global__ void k_col_merge(int n_exist, int brow0, const int *seg, const int *pool_m,
                             const float *pool_d, Key *g_key, int *dirty) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.x * kMergeWarps + (threadIdx.x >> 5);
   if (j >= n_exist) return;
   const int base = seg[2 * j], cnt = seg[2 * j + 1];
   if (!cnt) return;
   Key *lst = g_key + (size_t)j * kListW;
-  Key worst = lst[kListW - 1];
+  Key mine = lst[lane];
   bool changed = false;
-  for (int q = base; q < base + cnt; ++q) {
-    const Key ck = make_key(pool_d[q], brow0 + pool_m[q]);
-    if (!(ck < worst)) continue;
-    int pos = kListW - 1;
-    while (pos > 0 && ck < lst[pos - 1]) {
-      lst[pos] = lst[pos - 1];
-      --pos;
+  for (int c0 = 0; c0 < cnt; c0 += 32) {
+    const int c = c0 + lane;
+    const Key ck = c < cnt ? make_key(pool_d[base + c], brow0 + pool_m[base + c]) : ~(Key)0;
+    for (int src = 0; src < 32 && c0 + src < cnt; ++src) {
+      const Key k = __shfl_sync(0xffffffffu, ck, src);
+      const unsigned msk = __ballot_sync(0xffffffffu, k < mine);
+      if (!msk) continue;
+      changed = true;
+      const int pos = __ffs(msk) - 1;
+      const Key prev = __shfl_up_sync(0xffffffffu, mine, 1);
+      if (lane > pos) mine = prev;
+      else if (lane == pos) mine = k;
     }
-    lst[pos] = ck;
-    worst = lst[kListW - 1];
-    changed = true;
   }
-  if (changed) dirty[j] = 1;
+  if (changed) {
+    lst[lane] = mine;
+    if (lane == 0) dirty[j] = 1;
+  }
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
@@ -615,14 +646,14 @@ void launch_exact_screen(const DevState &st, int row0, int blk0, int nrows, int 
   if (nrows <= 0 || n <= 0) return;
   const int brow0 = row0 + blk0;  // global first row of the block
   const float coef = exact_bound_coef(st.d, exact_dh(st.d));
-  k_row_scan<<<nrows, kScanThreads, 0, s>>>(x.D, ldD, brow0, n, st.norms, coef, x.cand, ldD,
-                                            x.row_cnt, st.stat);
+  k_row_scan<<<nrows, kScanThreads, 0, s>>>(x.D, ldD, brow0, n, st.norms, st.snorms, coef,
+                                            x.cand, ldD, x.row_cnt, st.stat);
   note_launch();
   if (row0 > 0) {
     cudaMemsetAsync(x.counter, 0, sizeof(int), s);
     k_col_scan<<<cdiv(row0, kScanThreads), kScanThreads, 0, s>>>(
-        x.D, ldD, row0, brow0, nrows, st.norms, coef, st.g_key, x.pool_j, x.pool_m, x.pool_cap,
-        x.seg, x.counter, st.err, st.stat);
+        x.D, ldD, row0, brow0, nrows, st.norms, st.snorms, coef, st.g_key, x.pool_j, x.pool_m,
+        x.pool_cap, x.seg, x.counter, st.err, st.stat);
     note_launch();
   }
   k_row_dists<<<nrows, kPairWarps * 32, 0, s>>>(st.X, st.ld, st.d, st.norms, brow0, x.cand, ldD,
@@ -635,8 +666,8 @@ void launch_exact_screen(const DevState &st, int row0, int blk0, int nrows, int 
     k_pair_dists<<<4 * std::max(sms, 1), kPairWarps * 32, 0, s>>>(
         st.X, st.ld, st.d, st.norms, brow0, x.pool_j, x.pool_m, x.pool_d, x.counter, x.pool_cap);
     note_launch();
-    k_col_merge<<<cdiv(row0, kScanThreads), kScanThreads, 0, s>>>(row0, brow0, x.seg, x.pool_m,
-                                                                  x.pool_d, st.g_key, st.dirty);
+    k_col_merge<<<cdiv(row0, kMergeWarps), kMergeWarps * 32, 0, s>>>(
+        row0, brow0, x.seg, x.pool_m, x.pool_d, st.g_key, st.dirty);
     note_launch();
   }
 }

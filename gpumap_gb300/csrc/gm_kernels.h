@@ -17,6 +17,7 @@ struct DevState {
   int cosine = 0;
   float *X = nullptr;         // n_cap x ld, zero padded
   float *norms = nullptr;     // n_cap squared L2 norms
+  float *snorms = nullptr;    // n_cap sqrt of norms rounded up (exact-mode bounds)
   unsigned long long *g_key = nullptr;  // n_cap x 32 working lists, (dist bits << 32 | id)
   int *locks = nullptr;       // n_cap per-node locks (0 = free)
   int *dirty = nullptr;       // n_cap device dirty flags (0/1/2)
@@ -192,8 +193,18 @@ void launch_sgd(float *emb, const int *head, const int *tail, const float *eps,
                 int grid, float alpha0, float gamma, float a, float b, int n_epochs,
                 int neg_rate, uint64_t seed, cudaStream_t s,
                 unsigned long long *stat = nullptr);
+// All n_epochs epochs in one cooperative launch (one CTA of 512 threads per
+// SM) with a bounded grid barrier between epochs; bar: 2 device words,
+// cleared here; a barrier timeout sets kDevErrSpin in *err.
+cudaError_t launch_sgd_persistent(float *emb, const int *head, const int *tail,
+                                  const float *eps, float *next_s, float *next_n,
+                                  const int *iscal, const float *fscal, float alpha0,
+                                  float gamma, float a, float b, int n_epochs, int neg_rate,
+                                  uint64_t seed, unsigned *bar, unsigned *err, int device,
+                                  cudaStream_t s, unsigned long long *stat = nullptr);
 void launch_set_int(int *p, int v, cudaStream_t s);
 constexpr int kIscalN = 4;
+constexpr int kIscalBarrier = 8;  // iscal[8..9]: SGD grid-barrier words
 void launch_epoch_init(const float *eps, int nnz, int neg_rate, float *next_s,
                        float *next_n, cudaStream_t s);
 void launch_add_noise(float *emb, int n, const int *batch, int nb,

@@ -2,6 +2,8 @@
 // prepended), edge scheduling and negative-sampling SGD.  Restates the
 // reference's embedding_kernel.cuh and Impl::embed (impl.cuh:335-500) with
 // every count and threshold kept on the device (no host round trips).
+#include <algorithm>
+
 #include "gm_common.cuh"
 #include "gm_kernels.h"
 
@@ -258,85 +260,289 @@ GM_D float trunc_grad(float rounding, float x) {
   return __fsub_rn(__fadd_rn(rounding, x), rounding);
 }
 
-// One SGD epoch (reference optimize_batch_kernel, :509-589; Hogwild
-// updates, tail moved by rounded atomics, head accumulated then added).
+// One edge of one SGD epoch (reference optimize_batch_kernel, :509-589;
+// Hogwild updates, tail moved by rounded atomics, head accumulated then
+// added).  Embedding positions are read through L2 (ld.global.cg): in the
+// persistent kernel other SMs update them between epochs.  The positions of
+// the head, the tail and the first kNegAhead negative samples (rows drawn in
+// the same Philox order) are fetched together; a sample that is this edge's
+// own tail is advanced by this thread's tail update, which in sequential
+// order precedes the read.  powf(d2, b - 1) and powf(d2, b) share one log.
+constexpr int kNegAhead = 6;
+
+// 8-byte embedding row read through L2, issued where it stands (volatile, a
+// memory clobber): the sample positions are fetched ahead of their use.
+GM_D float2 ld_pos(const float *p) {
+  float2 v;
+  asm volatile("ld.global.cg.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p) : "memory");
+  return v;
+}
+
+// x mod n by a precomputed 64-bit reciprocal, exact for every 32-bit x and
+// n >= 1 (Lemire, Kaser and Kurz, "Faster remainder by direct computation",
+// 2019): M = floor((2^64 - 1) / n) + 1, x mod n = high64((M * x mod 2^64) * n).
+GM_D uint32_t fastmod(uint32_t x, uint64_t M, uint32_t n) {
+  return (uint32_t)__umul64hi(M * (uint64_t)x, (uint64_t)n);
+}
+
+// Number of negative samples of an active edge at epoch fe.
+GM_D int sgd_n_neg(float fe, float nn, float ep_neg) {
+  return (int)__fdiv_rn(__fsub_rn(fe, nn), ep_neg);
+}
+
+// Per-thread sample slots in shared memory: slot p of thread t at
+// [p * nthreads + t] (conflict free).
+struct SgdSlots {
+  int *r;
+  float2 *q;
+  int stride;
+};
+
+// One edge of one epoch.  The positions of the head, the tail and of the
+// first kNegAhead negative samples (rows from this edge's Philox stream,
+// blocks 0 and 1, words in order) are fetched together; samples are then
+// taken in order from shared-memory slots by a rolled loop (one copy of the
+// sample code: the kernel stays small enough for the instruction cache).  A
+// sample that is this edge's own tail is advanced by this thread's tail
+// update, which in sequential order precedes the read.  powf(d2, b - 1) and
+// powf(d2, b) share one log.
+GM_D void sgd_edge(float *emb, int row, int j, int kk, float ep, float &ns, float &nn, int n,
+                   uint64_t M, float rounding, float alpha, float fe, float gamma, float a,
+                   float b, float nsr_inv, uint64_t seed, const SgdSlots &sl,
+                   unsigned &my_edges, unsigned &my_negs) {
+  ++my_edges;
+  float *cp = emb + (size_t)j * 2;
+  float *op = emb + (size_t)kk * 2;
+  const float2 cpv = ld_pos(cp), opv = ld_pos(op);
+  float cur0 = cpv.x, cur1 = cpv.y;
+  const float ep_neg = __fmul_rn(ep, nsr_inv);
+  const int n_neg = sgd_n_neg(fe, nn, ep_neg);
+  int rr[kNegAhead];
+  float2 qq[kNegAhead];
+  if (n_neg > 0) {
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    uint32_t w[8];
+    philox_block((uint32_t)row, 0u, kTagNegSample, 0u, k0, k1, w);
+    if (n_neg > 4) philox_block((uint32_t)row, 1u, kTagNegSample, 0u, k0, k1, w + 4);
+#pragma unroll
+    for (int p = 0; p < kNegAhead; ++p) {
+      if (p < n_neg) {
+        rr[p] = (int)fastmod(w[p], M, (uint32_t)n);
+        qq[p] = ld_pos(emb + (size_t)rr[p] * 2);
+      }
+    }
+  }
+  const float dx = __fsub_rn(cur0, opv.x), dy = __fsub_rn(cur1, opv.y);
+  const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+  float attr = 0.0f;
+  if (d2 > 0.0f) {
+    const float lg = gm_logf(d2);
+    const float bm1 = __fsub_rn(b, 1.0f);
+    const float p_bm1 = bm1 == 0.0f ? 1.0f : gm_expf(__fmul_rn(bm1, lg));
+    const float p_b = b == 0.0f ? 1.0f : gm_expf(__fmul_rn(b, lg));
+    attr = __fdiv_rn(__fmul_rn(__fmul_rn(-2.0f, __fmul_rn(a, b)), p_bm1),
+                     __fadd_rn(__fmul_rn(a, p_b), 1.0f));
+  }
+  float g0 = __fmul_rn(fclip(__fmul_rn(attr, dx)), alpha);
+  float g1 = __fmul_rn(fclip(__fmul_rn(attr, dy)), alpha);
+  cur0 = __fadd_rn(cur0, g0);
+  cur1 = __fadd_rn(cur1, g1);
+  const float t0 = trunc_grad(rounding, -g0), t1 = trunc_grad(rounding, -g1);
+  atomicAdd(op, t0);
+  atomicAdd(op + 1, t1);
+  ns = __fadd_rn(ns, ep);
+  if (n_neg > 0) {
+#pragma unroll
+    for (int p = 0; p < kNegAhead; ++p) {
+      if (p < n_neg) {
+        sl.r[p * sl.stride] = rr[p];
+        sl.q[p * sl.stride] = qq[p];
+      }
+    }
+    const float two_gb = __fmul_rn(__fmul_rn(2.0f, gamma), b);
+    const float a4 = __fmul_rn(4.0f, alpha);
+    Philox g;  // draws past kNegAhead: the same stream from block 2 on
+    philox_init(g, seed, (uint32_t)row, kTagNegSample);
+    g.block = kNegAhead / 4;
+#pragma unroll 1
+    for (int p = 0; p < n_neg; ++p) {
+      int r;
+      float q0, q1;
+      if (p < kNegAhead) {
+        r = sl.r[p * sl.stride];
+        const float2 q = sl.q[p * sl.stride];
+        q0 = q.x, q1 = q.y;
+        if (r == kk) q0 = __fadd_rn(q0, t0), q1 = __fadd_rn(q1, t1);
+      } else {
+        r = (int)fastmod(philox_next(g), M, (uint32_t)n);
+        const float2 q = ld_pos(emb + (size_t)r * 2);
+        q0 = q.x, q1 = q.y;
+      }
+      if (r == j) continue;
+      const float ex = __fsub_rn(cur0, q0), ey = __fsub_rn(cur1, q1);
+      const float d2n = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+      float rep = 0.0f;
+      if (d2n > 0.0f)
+        rep = __fdiv_rn(two_gb, __fmul_rn(__fadd_rn(0.001f, d2n),
+                                          __fadd_rn(__fmul_rn(a, gm_powf(d2n, b)), 1.0f)));
+      const float h0 = (rep > 0.0f) ? __fmul_rn(fclip(__fmul_rn(rep, ex)), alpha) : a4;
+      const float h1 = (rep > 0.0f) ? __fmul_rn(fclip(__fmul_rn(rep, ey)), alpha) : a4;
+      cur0 = __fadd_rn(cur0, h0);
+      cur1 = __fadd_rn(cur1, h1);
+      g0 = __fadd_rn(g0, h0);
+      g1 = __fadd_rn(g1, h1);
+    }
+    nn = __fadd_rn(nn, __fmul_rn((float)n_neg, ep_neg));
+    my_negs += (unsigned)n_neg;
+  }
+  atomicAdd(cp, trunc_grad(rounding, g0));
+  atomicAdd(cp + 1, trunc_grad(rounding, g1));
+}
+
+// Edges [first, nnz) step stride of one epoch.  When res is set, the first
+// edge's state (head, tail, eps, next_s, next_n) lives in res for the whole
+// call instead of global memory.
+struct SgdResident {
+  int *j, *k;
+  float *ep, *ns, *nn;
+};
+GM_D void sgd_epoch_edges(float *emb, const int *head, const int *tail, const float *eps,
+                          float *next_s, float *next_n, int nnz, int n, uint64_t M,
+                          float rounding, float alpha, int epoch, float gamma, float a, float b,
+                          float nsr_inv, uint64_t seed, int first, int stride,
+                          const SgdSlots &sl, const SgdResident *res, unsigned &my_edges,
+                          unsigned &my_negs) {
+  const float fe = (float)epoch;
+#pragma unroll 1
+  for (int row = first; row < nnz; row += stride) {
+    const bool resident = res && row == first;
+    float ns = resident ? *res->ns : next_s[row];
+    if (ns > fe) continue;
+    float nn = resident ? *res->nn : next_n[row];
+    const int j = resident ? *res->j : head[row];
+    const int kk = resident ? *res->k : tail[row];
+    const float ep = resident ? *res->ep : eps[row];
+    sgd_edge(emb, row, j, kk, ep, ns, nn, n, M, rounding, alpha, fe, gamma, a, b, nsr_inv, seed, sl,
+             my_edges, my_negs);
+    if (resident) {
+      *res->ns = ns;
+      *res->nn = nn;
+    } else {
+      next_s[row] = ns;
+      next_n[row] = nn;
+    }
+  }
+}
+
+GM_D void sgd_stats(unsigned my_edges, unsigned my_negs, unsigned long long *stat) {
+  if (!stat) return;
+  for (int o = 16; o > 0; o >>= 1) {
+    my_edges += __shfl_xor_sync(0xffffffffu, my_edges, o);
+    my_negs += __shfl_xor_sync(0xffffffffu, my_negs, o);
+  }
+  if ((threadIdx.x & 31) == 0 && my_edges) {
+    atomicAdd(&stat[7], (unsigned long long)my_edges);
+    atomicAdd(&stat[8], (unsigned long long)my_negs);
+  }
+}
+
+// One SGD epoch per launch.
 __global__ void k_sgd_epoch(float *emb, const int *head, const int *tail,
                             const int *iscal, const float *eps, float *next_s,
                             float *next_n, float alpha, int epoch, float gamma, float a,
                             float b, float nsr_inv, uint64_t seed, const float *fscal,
                             unsigned long long *stat) {
-  const int nnz = iscal[IS_NNZ2];
-  const int n = iscal[IS_N];
+  __shared__ int s_r[kNegAhead * 256];
+  __shared__ float2 s_q[kNegAhead * 256];
   unsigned my_edges = 0, my_negs = 0;
-  const float rounding = fscal[FS_ROUND];
-  const float fe = (float)epoch;
-  const float bm1 = __fsub_rn(b, 1.0f);
-  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < nnz;
-       row += gridDim.x * blockDim.x) {
-    const float ns = next_s[row];
-    if (ns > fe) continue;
-    ++my_edges;
-    const float ep = eps[row];
-    const float ep_neg = __fmul_rn(ep, nsr_inv);
-    const int j = head[row], kk = tail[row];
-    float *cp = emb + (size_t)j * 2;
-    float *op = emb + (size_t)kk * 2;
-    float cur0 = cp[0], cur1 = cp[1];
-    const float o0 = op[0], o1 = op[1];
-    const float dx = __fsub_rn(cur0, o0), dy = __fsub_rn(cur1, o1);
-    const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-    float attr = 0.0f;
-    if (d2 > 0.0f)
-      attr = __fdiv_rn(__fmul_rn(__fmul_rn(-2.0f, __fmul_rn(a, b)), gm_powf(d2, bm1)),
-                       __fadd_rn(__fmul_rn(a, gm_powf(d2, b)), 1.0f));
-    float g0 = __fmul_rn(fclip(__fmul_rn(attr, dx)), alpha);
-    float g1 = __fmul_rn(fclip(__fmul_rn(attr, dy)), alpha);
-    cur0 = __fadd_rn(cur0, g0);
-    cur1 = __fadd_rn(cur1, g1);
-    atomicAdd(op, trunc_grad(rounding, -g0));
-    atomicAdd(op + 1, trunc_grad(rounding, -g1));
-    next_s[row] = __fadd_rn(ns, ep);
-    const float nn = next_n[row];
-    const int n_neg = (int)__fdiv_rn(__fsub_rn(fe, nn), ep_neg);
-    if (n_neg > 0) {
-      Philox g;
-      philox_init(g, seed, (uint32_t)row, kTagNegSample);
-      for (int p = 0; p < n_neg; ++p) {
-        const int r = (int)(philox_next(g) % (uint32_t)n);
-        if (r == j) continue;
-        const float q0 = emb[(size_t)r * 2], q1 = emb[(size_t)r * 2 + 1];
-        const float ex = __fsub_rn(cur0, q0), ey = __fsub_rn(cur1, q1);
-        const float d2n = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
-        float rep = 0.0f;
-        if (d2n > 0.0f)
-          rep = __fdiv_rn(__fmul_rn(__fmul_rn(2.0f, gamma), b),
-                          __fmul_rn(__fadd_rn(0.001f, d2n),
-                                    __fadd_rn(__fmul_rn(a, gm_powf(d2n, b)), 1.0f)));
-        const float h0 = (rep > 0.0f) ? __fmul_rn(fclip(__fmul_rn(rep, ex)), alpha)
-                                      : __fmul_rn(4.0f, alpha);
-        const float h1 = (rep > 0.0f) ? __fmul_rn(fclip(__fmul_rn(rep, ey)), alpha)
-                                      : __fmul_rn(4.0f, alpha);
-        cur0 = __fadd_rn(cur0, h0);
-        cur1 = __fadd_rn(cur1, h1);
-        g0 = __fadd_rn(g0, h0);
-        g1 = __fadd_rn(g1, h1);
+  const int n = iscal[IS_N];
+  const uint64_t M = ~0ull / (uint64_t)max(n, 1) + 1ull;
+  const SgdSlots sl{s_r + threadIdx.x, s_q + threadIdx.x, 256};
+  sgd_epoch_edges(emb, head, tail, eps, next_s, next_n, iscal[IS_NNZ2], n, M,
+                  fscal[FS_ROUND], alpha, epoch, gamma, a, b, nsr_inv, seed,
+                  blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, sl, nullptr,
+                  my_edges, my_negs);
+  sgd_stats(my_edges, my_negs, stat);
+}
+
+// Grid-wide barrier of a co-resident (cooperative) grid on a monotonic
+// arrival counter: the barrier after epoch e completes when the counter
+// reaches (e + 1) * gridDim.x.  The wait is bounded; on timeout it records
+// kDevErrSpin and returns false, and every block then leaves its epoch loop.
+constexpr unsigned kBarrierSpinLimit = 1u << 24;
+GM_D unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+// Arrival: the CTA's work for this epoch is done (bar.sync), made visible
+// (fence) and counted.
+GM_D void grid_arrive(unsigned *count) {
+  __syncthreads();
+  if (threadIdx.x == 0)
+    asm volatile("fence.acq_rel.gpu;\n\tred.relaxed.gpu.global.add.u32 [%0], 1;" ::"l"(count)
+                 : "memory");
+}
+// Wait until every CTA has arrived (count >= target); bounded.
+GM_D bool grid_wait(unsigned *count, unsigned target, unsigned *err) {
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    unsigned it = 0;
+    while (ld_acquire(count) < target) {
+      if (++it > kBarrierSpinLimit) {
+        ok = 0;
+        atomicOr(err, kDevErrSpin);
+        break;
       }
-      next_n[row] = __fadd_rn(nn, __fmul_rn((float)n_neg, ep_neg));
-      my_negs += (unsigned)n_neg;
+      __nanosleep(16);
     }
-    atomicAdd(cp, trunc_grad(rounding, g0));
-    atomicAdd(cp + 1, trunc_grad(rounding, g1));
+    s_ok = ok;
   }
-  if (stat) {
-    for (int o = 16; o > 0; o >>= 1) {
-      my_edges += __shfl_xor_sync(0xffffffffu, my_edges, o);
-      my_negs += __shfl_xor_sync(0xffffffffu, my_negs, o);
-    }
-    if ((threadIdx.x & 31) == 0 && my_edges) {
-      atomicAdd(&stat[7], (unsigned long long)my_edges);
-      atomicAdd(&stat[8], (unsigned long long)my_negs);
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// All epochs in one cooperative launch, a grid barrier between epochs (the
+// reference's kernel boundary): learning rate and seed advance exactly as the
+// host loop of the per-epoch form.  A thread's first edge keeps its indices
+// and sampling clocks in shared memory for the whole call.
+constexpr int kSgdThreads = 512;
+__global__ void __launch_bounds__(kSgdThreads)
+    k_sgd_persistent(float *emb, const int *head, const int *tail, const int *iscal,
+                     const float *eps, float *next_s, float *next_n, float alpha0, int n_epochs,
+                     float gamma, float a, float b, float nsr_inv, uint64_t seed,
+                     const float *fscal, unsigned *bar, unsigned *err,
+                     unsigned long long *stat) {
+  __shared__ int s_r[kNegAhead * kSgdThreads];
+  __shared__ float2 s_q[kNegAhead * kSgdThreads];
+  __shared__ int s_j[kSgdThreads], s_k[kSgdThreads];
+  __shared__ float s_ep[kSgdThreads], s_ns[kSgdThreads], s_nn[kSgdThreads];
+  const int nnz = iscal[IS_NNZ2], n = iscal[IS_N];
+  const uint64_t M = ~0ull / (uint64_t)max(n, 1) + 1ull;
+  const float rounding = fscal[FS_ROUND];
+  unsigned my_edges = 0, my_negs = 0;
+  const int tid = threadIdx.x;
+  const int first = blockIdx.x * blockDim.x + tid, stride = gridDim.x * blockDim.x;
+  if (first < nnz) {
+    s_j[tid] = head[first], s_k[tid] = tail[first], s_ep[tid] = eps[first];
+    s_ns[tid] = next_s[first], s_nn[tid] = next_n[first];
+  }
+  const SgdSlots sl{s_r + tid, s_q + tid, kSgdThreads};
+  const SgdResident res{s_j + tid, s_k + tid, s_ep + tid, s_ns + tid, s_nn + tid};
+  float alpha = alpha0;
+  for (int ep = 0; ep < n_epochs; ++ep) {
+    sgd_epoch_edges(emb, head, tail, eps, next_s, next_n, nnz, n, M, rounding, alpha, ep, gamma,
+                    a, b, nsr_inv, seed + (uint64_t)ep, first, stride, sl, &res, my_edges,
+                    my_negs);
+    alpha = __fmul_rn(alpha0, __fsub_rn(1.0f, __fdiv_rn((float)ep, (float)n_epochs)));
+    if (ep + 1 < n_epochs) {
+      grid_arrive(bar);
+      if (!grid_wait(bar, (unsigned)(ep + 1) * gridDim.x, err)) break;
     }
   }
+  if (first < nnz) next_s[first] = s_ns[tid], next_n[first] = s_nn[tid];
+  sgd_stats(my_edges, my_negs, stat);
 }
 
 __global__ void k_set_int(int *p, int v) { *p = v; }
@@ -532,6 +738,38 @@ void launch_sgd(float *emb, const int *head, const int *tail, const float *eps,
     alpha = alpha0 * (1.0f - (float)ep / (float)n_epochs);
     cur_seed += 1;
   }
+}
+
+int sgd_persistent_grid(int device) {
+  static int grid[64] = {0};
+  if (device < 0 || device >= 64) return 0;
+  if (!grid[device]) {
+    int sms = 0, occ = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_sgd_persistent, kSgdThreads, 0);
+    grid[device] = std::max(1, sms) * std::max(1, std::min(occ, 1));
+  }
+  return grid[device];
+}
+
+cudaError_t launch_sgd_persistent(float *emb, const int *head, const int *tail,
+                                  const float *eps, float *next_s, float *next_n,
+                                  const int *iscal, const float *fscal, float alpha0,
+                                  float gamma, float a, float b, int n_epochs, int neg_rate,
+                                  uint64_t seed, unsigned *bar, unsigned *err, int device,
+                                  cudaStream_t s, unsigned long long *stat) {
+  if (n_epochs <= 0) return cudaSuccess;
+  const int grid = sgd_persistent_grid(device);
+  if (grid <= 0) return cudaErrorInvalidDevice;
+  cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  float nsr_inv = 1.0f / (float)neg_rate;
+  void *args[] = {&emb, &head, &tail, &iscal, &eps, &next_s, &next_n, &alpha0, &n_epochs,
+                  &gamma, &a, &b, &nsr_inv, &seed, &fscal, &bar, &err, &stat};
+  e = cudaLaunchCooperativeKernel((const void *)k_sgd_persistent, dim3(grid), dim3(kSgdThreads),
+                                  args, 0, s);
+  note_launch();
+  return e;
 }
 
 void launch_add_noise(float *emb, int n, const int *batch, int nb, float noise_scale,

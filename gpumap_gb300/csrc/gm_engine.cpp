@@ -656,11 +656,13 @@ uint32_t Session::embed(uint32_t n_ops) {
 
 // The max_epoch SGD epochs of one embedding call: one cooperative launch
 // with a grid barrier between epochs (sizes are read from device scalars).
+// t_col (free once the schedule is built) holds the edge grouping and
+// ipartial its bins.
 void Session::run_sgd() {
   if (p_.max_epoch == 0) return;
   ck(launch_sgd_persistent(st_.emb, es_.t_row, es_.flag_tail, es_.t_val, es_.next_s, es_.next_n,
                            es_.iscal, es_.fscal, p_.alpha, 1.0f, p_.a, p_.b, (int)p_.max_epoch,
-                           (int)p_.negative_sample_rate, 42ull,
+                           (int)p_.negative_sample_rate, 42ull, es_.t_col, es_.ipartial,
                            (unsigned *)(es_.iscal + kIscalBarrier), st_.err, device_, stream_,
                            st_.stat),
      "SGD launch");

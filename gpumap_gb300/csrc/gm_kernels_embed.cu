@@ -268,7 +268,7 @@ GM_D float trunc_grad(float rounding, float x) {
 // the same Philox order) are fetched together; a sample that is this edge's
 // own tail is advanced by this thread's tail update, which in sequential
 // order precedes the read.  powf(d2, b - 1) and powf(d2, b) share one log.
-constexpr int kNegAhead = 6;
+constexpr int kNegAhead = 8;
 
 // 8-byte embedding row read through L2, issued where it stands (volatile, a
 // memory clobber): the sample positions are fetched ahead of their use.
@@ -290,26 +290,16 @@ GM_D int sgd_n_neg(float fe, float nn, float ep_neg) {
   return (int)__fdiv_rn(__fsub_rn(fe, nn), ep_neg);
 }
 
-// Per-thread sample slots in shared memory: slot p of thread t at
-// [p * nthreads + t] (conflict free).
-struct SgdSlots {
-  int *r;
-  float2 *q;
-  int stride;
-};
-
 // One edge of one epoch.  The positions of the head, the tail and of the
 // first kNegAhead negative samples (rows from this edge's Philox stream,
-// blocks 0 and 1, words in order) are fetched together; samples are then
-// taken in order from shared-memory slots by a rolled loop (one copy of the
-// sample code: the kernel stays small enough for the instruction cache).  A
-// sample that is this edge's own tail is advanced by this thread's tail
-// update, which in sequential order precedes the read.  powf(d2, b - 1) and
-// powf(d2, b) share one log.
+// blocks 0 and 1, words in order, computed directly into registers) are
+// fetched together, ahead of the sequential updates.  A sample that is this
+// edge's own tail is advanced by this thread's tail update, which in
+// sequential order precedes the read.  powf(d2, b - 1) and powf(d2, b) share
+// one log.
 GM_D void sgd_edge(float *emb, int row, int j, int kk, float ep, float &ns, float &nn, int n,
                    uint64_t M, float rounding, float alpha, float fe, float gamma, float a,
-                   float b, float nsr_inv, uint64_t seed, const SgdSlots &sl,
-                   unsigned &my_edges, unsigned &my_negs) {
+                   float b, float nsr_inv, uint64_t seed, unsigned &my_edges, unsigned &my_negs) {
   ++my_edges;
   float *cp = emb + (size_t)j * 2;
   float *op = emb + (size_t)kk * 2;
@@ -352,33 +342,11 @@ GM_D void sgd_edge(float *emb, int row, int j, int kk, float ep, float &ns, floa
   atomicAdd(op + 1, t1);
   ns = __fadd_rn(ns, ep);
   if (n_neg > 0) {
-#pragma unroll
-    for (int p = 0; p < kNegAhead; ++p) {
-      if (p < n_neg) {
-        sl.r[p * sl.stride] = rr[p];
-        sl.q[p * sl.stride] = qq[p];
-      }
-    }
     const float two_gb = __fmul_rn(__fmul_rn(2.0f, gamma), b);
     const float a4 = __fmul_rn(4.0f, alpha);
-    Philox g;  // draws past kNegAhead: the same stream from block 2 on
-    philox_init(g, seed, (uint32_t)row, kTagNegSample);
-    g.block = kNegAhead / 4;
-#pragma unroll 1
-    for (int p = 0; p < n_neg; ++p) {
-      int r;
-      float q0, q1;
-      if (p < kNegAhead) {
-        r = sl.r[p * sl.stride];
-        const float2 q = sl.q[p * sl.stride];
-        q0 = q.x, q1 = q.y;
-        if (r == kk) q0 = __fadd_rn(q0, t0), q1 = __fadd_rn(q1, t1);
-      } else {
-        r = (int)fastmod(philox_next(g), M, (uint32_t)n);
-        const float2 q = ld_pos(emb + (size_t)r * 2);
-        q0 = q.x, q1 = q.y;
-      }
-      if (r == j) continue;
+    // one negative sample: repulsion from q, head moved in sequence
+    auto negative = [&](int r, float q0, float q1) {
+      if (r == j) return;
       const float ex = __fsub_rn(cur0, q0), ey = __fsub_rn(cur1, q1);
       const float d2n = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
       float rep = 0.0f;
@@ -391,6 +359,25 @@ GM_D void sgd_edge(float *emb, int row, int j, int kk, float ep, float &ns, floa
       cur1 = __fadd_rn(cur1, h1);
       g0 = __fadd_rn(g0, h0);
       g1 = __fadd_rn(g1, h1);
+    };
+#pragma unroll
+    for (int p = 0; p < kNegAhead; ++p) {
+      if (p < n_neg) {
+        const bool own = rr[p] == kk;
+        negative(rr[p], own ? __fadd_rn(qq[p].x, t0) : qq[p].x,
+                 own ? __fadd_rn(qq[p].y, t1) : qq[p].y);
+      }
+    }
+    if (n_neg > kNegAhead) {
+      // draws past kNegAhead: the same stream from block 2 on
+      Philox g;
+      philox_init(g, seed, (uint32_t)row, kTagNegSample);
+      g.block = kNegAhead / 4;
+      for (int p = kNegAhead; p < n_neg; ++p) {
+        const int r = (int)fastmod(philox_next(g), M, (uint32_t)n);
+        const float2 q = ld_pos(emb + (size_t)r * 2);
+        negative(r, q.x, q.y);
+      }
     }
     nn = __fadd_rn(nn, __fmul_rn((float)n_neg, ep_neg));
     my_negs += (unsigned)n_neg;
@@ -399,38 +386,21 @@ GM_D void sgd_edge(float *emb, int row, int j, int kk, float ep, float &ns, floa
   atomicAdd(cp + 1, trunc_grad(rounding, g1));
 }
 
-// Edges [first, nnz) step stride of one epoch.  When res is set, the first
-// edge's state (head, tail, eps, next_s, next_n) lives in res for the whole
-// call instead of global memory.
-struct SgdResident {
-  int *j, *k;
-  float *ep, *ns, *nn;
-};
+// Edges [first, nnz) step stride of one epoch, state in global memory.
 GM_D void sgd_epoch_edges(float *emb, const int *head, const int *tail, const float *eps,
                           float *next_s, float *next_n, int nnz, int n, uint64_t M,
                           float rounding, float alpha, int epoch, float gamma, float a, float b,
                           float nsr_inv, uint64_t seed, int first, int stride,
-                          const SgdSlots &sl, const SgdResident *res, unsigned &my_edges,
-                          unsigned &my_negs) {
+                          unsigned &my_edges, unsigned &my_negs) {
   const float fe = (float)epoch;
-#pragma unroll 1
   for (int row = first; row < nnz; row += stride) {
-    const bool resident = res && row == first;
-    float ns = resident ? *res->ns : next_s[row];
+    float ns = next_s[row];
     if (ns > fe) continue;
-    float nn = resident ? *res->nn : next_n[row];
-    const int j = resident ? *res->j : head[row];
-    const int kk = resident ? *res->k : tail[row];
-    const float ep = resident ? *res->ep : eps[row];
-    sgd_edge(emb, row, j, kk, ep, ns, nn, n, M, rounding, alpha, fe, gamma, a, b, nsr_inv, seed, sl,
-             my_edges, my_negs);
-    if (resident) {
-      *res->ns = ns;
-      *res->nn = nn;
-    } else {
-      next_s[row] = ns;
-      next_n[row] = nn;
-    }
+    float nn = next_n[row];
+    sgd_edge(emb, row, head[row], tail[row], eps[row], ns, nn, n, M, rounding, alpha, fe, gamma, a,
+             b, nsr_inv, seed, my_edges, my_negs);
+    next_s[row] = ns;
+    next_n[row] = nn;
   }
 }
 
@@ -452,16 +422,13 @@ __global__ void k_sgd_epoch(float *emb, const int *head, const int *tail,
                             float *next_n, float alpha, int epoch, float gamma, float a,
                             float b, float nsr_inv, uint64_t seed, const float *fscal,
                             unsigned long long *stat) {
-  __shared__ int s_r[kNegAhead * 256];
-  __shared__ float2 s_q[kNegAhead * 256];
   unsigned my_edges = 0, my_negs = 0;
   const int n = iscal[IS_N];
   const uint64_t M = ~0ull / (uint64_t)max(n, 1) + 1ull;
-  const SgdSlots sl{s_r + threadIdx.x, s_q + threadIdx.x, 256};
   sgd_epoch_edges(emb, head, tail, eps, next_s, next_n, iscal[IS_NNZ2], n, M,
                   fscal[FS_ROUND], alpha, epoch, gamma, a, b, nsr_inv, seed,
-                  blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, sl, nullptr,
-                  my_edges, my_negs);
+                  blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, my_edges,
+                  my_negs);
   sgd_stats(my_edges, my_negs, stat);
 }
 
@@ -505,44 +472,98 @@ GM_D bool grid_wait(unsigned *count, unsigned target, unsigned *err) {
 
 // All epochs in one cooperative launch, a grid barrier between epochs (the
 // reference's kernel boundary): learning rate and seed advance exactly as the
-// host loop of the per-epoch form.  A thread's first edge keeps its indices
-// and sampling clocks in shared memory for the whole call.
+// host loop of the per-epoch form.  A thread's first kRegEdges edges keep
+// their indices and sampling clocks in registers for the whole call.
+constexpr int kRegEdges = 2;
 constexpr int kSgdThreads = 512;
 __global__ void __launch_bounds__(kSgdThreads)
     k_sgd_persistent(float *emb, const int *head, const int *tail, const int *iscal,
                      const float *eps, float *next_s, float *next_n, float alpha0, int n_epochs,
                      float gamma, float a, float b, float nsr_inv, uint64_t seed,
-                     const float *fscal, unsigned *bar, unsigned *err,
+                     const float *fscal, const int *perm, unsigned *bar, unsigned *err,
                      unsigned long long *stat) {
-  __shared__ int s_r[kNegAhead * kSgdThreads];
-  __shared__ float2 s_q[kNegAhead * kSgdThreads];
-  __shared__ int s_j[kSgdThreads], s_k[kSgdThreads];
-  __shared__ float s_ep[kSgdThreads], s_ns[kSgdThreads], s_nn[kSgdThreads];
   const int nnz = iscal[IS_NNZ2], n = iscal[IS_N];
   const uint64_t M = ~0ull / (uint64_t)max(n, 1) + 1ull;
   const float rounding = fscal[FS_ROUND];
   unsigned my_edges = 0, my_negs = 0;
-  const int tid = threadIdx.x;
-  const int first = blockIdx.x * blockDim.x + tid, stride = gridDim.x * blockDim.x;
-  if (first < nnz) {
-    s_j[tid] = head[first], s_k[tid] = tail[first], s_ep[tid] = eps[first];
-    s_ns[tid] = next_s[first], s_nn[tid] = next_n[first];
+  const int first = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  // slot i of the grid handles edge perm[i] (edges grouped by sampling period,
+  // so that a warp's lanes tend to be active in the same epochs)
+  int rrow[kRegEdges], rj[kRegEdges], rk[kRegEdges];
+  float rep[kRegEdges], rns[kRegEdges], rnn[kRegEdges];
+#pragma unroll
+  for (int t = 0; t < kRegEdges; ++t) {
+    const int slot = first + t * stride;
+    if (slot < nnz) {
+      const int row = perm ? perm[slot] : slot;
+      rrow[t] = row;
+      rj[t] = head[row], rk[t] = tail[row], rep[t] = eps[row];
+      rns[t] = next_s[row], rnn[t] = next_n[row];
+    }
   }
-  const SgdSlots sl{s_r + tid, s_q + tid, kSgdThreads};
-  const SgdResident res{s_j + tid, s_k + tid, s_ep + tid, s_ns + tid, s_nn + tid};
   float alpha = alpha0;
   for (int ep = 0; ep < n_epochs; ++ep) {
-    sgd_epoch_edges(emb, head, tail, eps, next_s, next_n, nnz, n, M, rounding, alpha, ep, gamma,
-                    a, b, nsr_inv, seed + (uint64_t)ep, first, stride, sl, &res, my_edges,
-                    my_negs);
+    const float fe = (float)ep;
+    const uint64_t sd = seed + (uint64_t)ep;
+#pragma unroll
+    for (int t = 0; t < kRegEdges; ++t) {
+      if (first + t * stride < nnz && rns[t] <= fe)
+        sgd_edge(emb, rrow[t], rj[t], rk[t], rep[t], rns[t], rnn[t], n, M, rounding, alpha, fe,
+                 gamma, a, b, nsr_inv, sd, my_edges, my_negs);
+    }
+    for (int slot = first + kRegEdges * stride; slot < nnz; slot += stride) {
+      const int row = perm ? perm[slot] : slot;
+      float ns = next_s[row];
+      if (ns > fe) continue;
+      float nn = next_n[row];
+      sgd_edge(emb, row, head[row], tail[row], eps[row], ns, nn, n, M, rounding, alpha, fe, gamma,
+               a, b, nsr_inv, sd, my_edges, my_negs);
+      next_s[row] = ns;
+      next_n[row] = nn;
+    }
     alpha = __fmul_rn(alpha0, __fsub_rn(1.0f, __fdiv_rn((float)ep, (float)n_epochs)));
     if (ep + 1 < n_epochs) {
       grid_arrive(bar);
       if (!grid_wait(bar, (unsigned)(ep + 1) * gridDim.x, err)) break;
     }
   }
-  if (first < nnz) next_s[first] = s_ns[tid], next_n[first] = s_nn[tid];
+#pragma unroll
+  for (int t = 0; t < kRegEdges; ++t)
+    if (first + t * stride < nnz) next_s[rrow[t]] = rns[t], next_n[rrow[t]] = rnn[t];
   sgd_stats(my_edges, my_negs, stat);
+}
+
+// Edge grouping by sampling period: counting sort of the edges on
+// min(floor(8 * epochs_per_sample), kEpsBins - 1) into perm.
+constexpr int kEpsBins = 256;
+GM_D int eps_bin(float e) {
+  const float v = __fmul_rn(e, 8.0f);
+  return v < (float)(kEpsBins - 1) ? max((int)v, 0) : kEpsBins - 1;
+}
+__global__ void k_eps_hist(const float *eps, const int *iscal, int *bins) {
+  __shared__ int h[kEpsBins];
+  for (int i = threadIdx.x; i < kEpsBins; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  const int nnz = iscal[IS_NNZ2];
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += gridDim.x * blockDim.x)
+    atomicAdd(&h[eps_bin(eps[q])], 1);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kEpsBins; i += blockDim.x)
+    if (h[i]) atomicAdd(&bins[i], h[i]);
+}
+__global__ void k_eps_scan(int *bins) {  // one block of kEpsBins threads
+  __shared__ int v[kEpsBins];
+  const int t = threadIdx.x;
+  v[t] = bins[t];
+  __syncthreads();
+  int acc = 0;
+  for (int i = 0; i < t; ++i) acc += v[i];
+  bins[t] = acc;
+}
+__global__ void k_eps_scatter(const float *eps, const int *iscal, int *bins, int *perm) {
+  const int nnz = iscal[IS_NNZ2];
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += gridDim.x * blockDim.x)
+    perm[atomicAdd(&bins[eps_bin(eps[q])], 1)] = q;
 }
 
 __global__ void k_set_int(int *p, int v) { *p = v; }
@@ -756,16 +777,26 @@ cudaError_t launch_sgd_persistent(float *emb, const int *head, const int *tail,
                                   const float *eps, float *next_s, float *next_n,
                                   const int *iscal, const float *fscal, float alpha0,
                                   float gamma, float a, float b, int n_epochs, int neg_rate,
-                                  uint64_t seed, unsigned *bar, unsigned *err, int device,
-                                  cudaStream_t s, unsigned long long *stat) {
+                                  uint64_t seed, int *perm, int *bins, unsigned *bar,
+                                  unsigned *err, int device, cudaStream_t s,
+                                  unsigned long long *stat) {
   if (n_epochs <= 0) return cudaSuccess;
   const int grid = sgd_persistent_grid(device);
   if (grid <= 0) return cudaErrorInvalidDevice;
   cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
+  if (perm) {
+    e = cudaMemsetAsync(bins, 0, kEpsBins * sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    k_eps_hist<<<grid, 256, 0, s>>>(eps, iscal, bins);
+    k_eps_scan<<<1, kEpsBins, 0, s>>>(bins);
+    k_eps_scatter<<<grid, 256, 0, s>>>(eps, iscal, bins, perm);
+    note_launch(3);
+  }
   float nsr_inv = 1.0f / (float)neg_rate;
+  const int *cperm = perm;
   void *args[] = {&emb, &head, &tail, &iscal, &eps, &next_s, &next_n, &alpha0, &n_epochs,
-                  &gamma, &a, &b, &nsr_inv, &seed, &fscal, &bar, &err, &stat};
+                  &gamma, &a, &b, &nsr_inv, &seed, &fscal, &cperm, &bar, &err, &stat};
   e = cudaLaunchCooperativeKernel((const void *)k_sgd_persistent, dim3(grid), dim3(kSgdThreads),
                                   args, 0, s);
   note_launch();

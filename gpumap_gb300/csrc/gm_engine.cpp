@@ -144,6 +144,7 @@ Session::Session(const gm_params &p) : p_(p) {
       xs_.pool_m = (int *)dalloc((size_t)xs_.pool_cap * sizeof(int));
       xs_.pool_d = (float *)dalloc((size_t)xs_.pool_cap * sizeof(float));
       xs_.seg = (int *)dalloc(Nm * 2 * sizeof(int));
+      xs_.slab = (int *)dalloc(((size_t)ex_block_ / 32 + 1) * Nm * sizeof(int));
       xs_.counter = (int *)dalloc(16 * sizeof(int));
     }
   } catch (...) {

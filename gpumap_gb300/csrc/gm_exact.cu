@@ -291,9 +291,9 @@ GM_D float pair_bound(float coef, float sa, float sb, float na, float nb) {
 // Per block of batch rows (brow0 .. brow0 + nrows) against columns [0, n):
 //  k_row_scan    CTA per batch row: threshold T (32nd smallest upper bound),
 //                candidate columns whose lower bound reaches T
-//  k_col_scan    thread per existing row j < n_exist: batch rows whose lower
-//                bound reaches j's current 32nd distance, as a contiguous
-//                segment of the column pool
+//  k_col_*       existing rows j < n_exist: batch rows whose lower bound
+//                reaches j's current 32nd distance, as a contiguous segment
+//                of the column pool
 //  k_row_dists   canonical distances of the row candidates
 //  k_pair_dists  canonical distances of the column pool
 //  k_row_select  warp per batch row: exact top-32 keys of its candidates
@@ -380,55 +380,87 @@ __global__ void __launch_bounds__(kScanThreads)
   }
 }
 
-constexpr int kColRows = 1024;  // batch rows whose norms a col-scan CTA caches
+// Column direction in three steps over slabs of kSlab batch rows:
+//  k_col_count  thread per (existing row j, slab): hits of the bound test
+//  k_col_place  thread per j: total, a contiguous pool segment (one atomic),
+//               per-slab offsets
+//  k_col_write  thread per (j, slab): the same test again, pairs written
+// The two passes evaluate the identical test on identical inputs.
+constexpr int kSlab = 32;
+GM_D bool col_hit(const float *D, long ldD, int j, int ml, float w, float coef, float sj, float nj,
+                  float sm, float nm) {
+  return __fsub_rd(D[(long)ml * ldD + j], pair_bound(coef, sj, sm, nj, nm)) <= w;
+}
 __global__ void __launch_bounds__(kScanThreads)
-    k_col_scan(const float *D, long ldD, int n_exist, int brow0, int nrows, const float *norms,
-               const float *snorms, float coef, const Key *g_key, int *pool_j, int *pool_m,
-               long pool_cap, int *seg, int *counter, unsigned *err, unsigned long long *stat) {
-  __shared__ float s_n[kColRows], s_s[kColRows];
+    k_col_count(const float *D, long ldD, int n_exist, int brow0, int nrows, const float *norms,
+                const float *snorms, float coef, const Key *g_key, int *slab_cnt) {
+  __shared__ float s_n[kSlab], s_s[kSlab];
+  const int sl = blockIdx.y, m0 = sl * kSlab, mr = min(kSlab, nrows - m0);
+  if (threadIdx.x < mr) {
+    s_n[threadIdx.x] = norms[brow0 + m0 + threadIdx.x];
+    s_s[threadIdx.x] = snorms[brow0 + m0 + threadIdx.x];
+  }
+  __syncthreads();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = j < n_exist;
-  const float w = live ? key_dist(g_key[(size_t)j * kListW + kListW - 1]) : 0.0f;
-  const float nj = live ? norms[j] : 0.0f, sj = live ? snorms[j] : 0.0f;
+  if (j >= n_exist) return;
+  const float w = key_dist(g_key[(size_t)j * kListW + kListW - 1]);
+  const float nj = norms[j], sj = snorms[j];
   int cnt = 0;
-  for (int m0 = 0; m0 < nrows; m0 += kColRows) {
-    const int mr = min(kColRows, nrows - m0);
-    __syncthreads();
-    for (int i = threadIdx.x; i < mr; i += blockDim.x) {
-      s_n[i] = norms[brow0 + m0 + i];
-      s_s[i] = snorms[brow0 + m0 + i];
-    }
-    __syncthreads();
-    if (live) {
-      const float *Dc = D + (long)m0 * ldD + j;
 #pragma unroll 8
-      for (int i = 0; i < mr; ++i)
-        cnt += __fsub_rd(Dc[(long)i * ldD], pair_bound(coef, sj, s_s[i], nj, s_n[i])) <= w;
-    }
-  }
-  if (!live) return;
+  for (int i = 0; i < mr; ++i) cnt += col_hit(D, ldD, j, m0 + i, w, coef, sj, nj, s_s[i], s_n[i]);
+  slab_cnt[(size_t)sl * n_exist + j] = cnt;
+}
+__global__ void k_col_place(int n_exist, int nslabs, int *slab_cnt, long pool_cap, int *seg,
+                            int *counter, unsigned *err, unsigned long long *stat) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_exist) return;
+  int tot = 0;
+  for (int sl = 0; sl < nslabs; ++sl) tot += slab_cnt[(size_t)sl * n_exist + j];
   int base = 0;
-  if (cnt) {
-    base = atomicAdd(counter, cnt);
-    if ((long)base + cnt > pool_cap) {
+  if (tot) {
+    base = atomicAdd(counter, tot);
+    if ((long)base + tot > pool_cap) {
       atomicOr(err, kDevErrOverflow);
-      cnt = 0;
-    } else {
-      // second pass (rare hits): same test, norms from global memory
-      int q = base;
-      for (int ml = 0; ml < nrows && q < base + cnt; ++ml) {
-        if (__fsub_rd(D[(long)ml * ldD + j],
-                      pair_bound(coef, sj, snorms[brow0 + ml], nj, norms[brow0 + ml])) <= w) {
-          pool_j[q] = j;
-          pool_m[q] = ml;
-          ++q;
-        }
-      }
-      if (stat) atomicAdd(&stat[6], (unsigned long long)cnt);
+      tot = 0;
+      base = -1;  // nothing is written for this row
+    } else if (stat) {
+      atomicAdd(&stat[6], (unsigned long long)tot);
     }
   }
-  seg[2 * j] = base;
-  seg[2 * j + 1] = cnt;
+  // slab counts become slab offsets (-1: skip)
+  int off = base;
+  for (int sl = 0; sl < nslabs; ++sl) {
+    const int c = slab_cnt[(size_t)sl * n_exist + j];
+    slab_cnt[(size_t)sl * n_exist + j] = base < 0 ? -1 : off;
+    off += c;
+  }
+  seg[2 * j] = base < 0 ? 0 : base;
+  seg[2 * j + 1] = tot;
+}
+__global__ void __launch_bounds__(kScanThreads)
+    k_col_write(const float *D, long ldD, int n_exist, int brow0, int nrows, const float *norms,
+                const float *snorms, float coef, const Key *g_key, const int *slab_off,
+                int *pool_j, int *pool_m) {
+  __shared__ float s_n[kSlab], s_s[kSlab];
+  const int sl = blockIdx.y, m0 = sl * kSlab, mr = min(kSlab, nrows - m0);
+  if (threadIdx.x < mr) {
+    s_n[threadIdx.x] = norms[brow0 + m0 + threadIdx.x];
+    s_s[threadIdx.x] = snorms[brow0 + m0 + threadIdx.x];
+  }
+  __syncthreads();
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n_exist) return;
+  int q = slab_off[(size_t)sl * n_exist + j];
+  if (q < 0) return;
+  const float w = key_dist(g_key[(size_t)j * kListW + kListW - 1]);
+  const float nj = norms[j], sj = snorms[j];
+  for (int i = 0; i < mr; ++i) {
+    if (col_hit(D, ldD, j, m0 + i, w, coef, sj, nj, s_s[i], s_n[i])) {
+      pool_j[q] = j;
+      pool_m[q] = m0 + i;
+      ++q;
+    }
+  }
 }
 
 // Stages rows ra / rb (this lane's pair; dummies for idle lanes) 32 features
@@ -651,10 +683,15 @@ void launch_exact_screen(const DevState &st, int row0, int blk0, int nrows, int 
   note_launch();
   if (row0 > 0) {
     cudaMemsetAsync(x.counter, 0, sizeof(int), s);
-    k_col_scan<<<cdiv(row0, kScanThreads), kScanThreads, 0, s>>>(
-        x.D, ldD, row0, brow0, nrows, st.norms, st.snorms, coef, st.g_key, x.pool_j, x.pool_m,
-        x.pool_cap, x.seg, x.counter, st.err, st.stat);
-    note_launch();
+    const int nslabs = cdiv(nrows, kSlab);
+    const dim3 g2(cdiv(row0, kScanThreads), nslabs);
+    k_col_count<<<g2, kScanThreads, 0, s>>>(x.D, ldD, row0, brow0, nrows, st.norms, st.snorms,
+                                            coef, st.g_key, x.slab);
+    k_col_place<<<cdiv(row0, kScanThreads), kScanThreads, 0, s>>>(
+        row0, nslabs, x.slab, x.pool_cap, x.seg, x.counter, st.err, st.stat);
+    k_col_write<<<g2, kScanThreads, 0, s>>>(x.D, ldD, row0, brow0, nrows, st.norms, st.snorms,
+                                            coef, st.g_key, x.slab, x.pool_j, x.pool_m);
+    note_launch(3);
   }
   k_row_dists<<<nrows, kPairWarps * 32, 0, s>>>(st.X, st.ld, st.d, st.norms, brow0, x.cand, ldD,
                                                x.row_cnt, x.cand_d);

@@ -117,6 +117,7 @@ struct ExactScreen {
   int *pool_j = nullptr, *pool_m = nullptr;  // column-direction pairs
   float *pool_d = nullptr;
   int *seg = nullptr;     // n_cap x 2: (first pair, pairs) per existing row
+  int *slab = nullptr;    // (rows / 32 + 1) x n_cap per-slab counts, then offsets
   int *counter = nullptr; // pairs in the pool
   long pool_cap = 0;
 };

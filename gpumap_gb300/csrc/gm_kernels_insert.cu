@@ -13,43 +13,43 @@ namespace {
 // ||x||^2 for each batch row by a sequential fma chain over the features.
 // Cosine: normalises the row in place first and stores 1.0
 // (reference: preprocess_l2_norms_kernel, insertion_kernel.cuh:31-81).
-// Squared norms of 32 rows per CTA: the rows are staged in shared memory a
-// chunk of up to kNormChunk features at a time by coalesced loads of all 128
-// threads, then warp 0 runs the 32 sequential fma chains (lane l reads row l:
-// odd row pitch, conflict free).  Cosine rows are normalised in place, and
-// snorms gets sqrt(norm) rounded up.
-constexpr int kNormRows = 32, kNormChunk = 1024;
-__global__ void __launch_bounds__(128)
+// Squared norms of kNormRows rows per CTA: the rows are staged in shared
+// memory a chunk of up to kNormChunk features at a time by float4 loads of
+// all threads (rows are 16-byte aligned, ld a multiple of 4), then lanes
+// 0..kNormRows-1 of warp 0 run the sequential fma chains.  Cosine rows are
+// normalised in place, and snorms gets sqrt(norm) rounded up.
+constexpr int kNormRows = 8, kNormChunk = 1024;
+__global__ void __launch_bounds__(256)
     k_row_norms(float *X, float *norms, float *snorms, int ld, int d, int row0, int nrows,
                 int cosine) {
-  extern __shared__ float tile[];  // kNormRows x (chunk + 1)
+  __shared__ __align__(16) float tile[kNormRows][kNormChunk + 4];
   __shared__ float s_scale[kNormRows];
   const int r0 = blockIdx.x * kNormRows;
   const int rows = min(kNormRows, nrows - r0);
-  const int chunk = min(d, kNormChunk), pitch = chunk + 1;
   const int tid = threadIdx.x, lane = tid & 31;
   float acc = 0.0f;
-  for (int c0 = 0; c0 < d; c0 += chunk) {
-    const int w = min(chunk, d - c0);
-    for (int i = tid; i < rows * w; i += blockDim.x) {
-      const int r = i / w, c = i - r * w;
-      tile[r * pitch + c] = X[(size_t)(row0 + r0 + r) * ld + c0 + c];
+  for (int c0 = 0; c0 < d; c0 += kNormChunk) {
+    const int w = min(kNormChunk, d - c0);
+    const int w4 = (w + 3) >> 2;  // float4 columns (the row padding is zero)
+    for (int r = 0; r < rows; ++r) {
+      const float4 *src = reinterpret_cast<const float4 *>(X + (size_t)(row0 + r0 + r) * ld + c0);
+      for (int c = tid; c < w4; c += blockDim.x)
+        *reinterpret_cast<float4 *>(&tile[r][4 * c]) = src[c];
     }
     __syncthreads();
-    if (tid < 32 && lane < rows)
+    if (tid < rows)
       for (int c = 0; c < w; ++c) {
-        const float v = tile[lane * pitch + c];
+        const float v = tile[lane][c];
         acc = __fmaf_rn(v, v, acc);
       }
     __syncthreads();
   }
-  if (tid < 32 && lane < rows) {
+  if (tid < rows) {
     const size_t row = (size_t)(row0 + r0 + lane);
     float nv = acc;
     s_scale[lane] = 0.0f;
     if (cosine) {
-      const float nrm = __fsqrt_rn(acc);
-      s_scale[lane] = nrm;
+      s_scale[lane] = __fsqrt_rn(acc);
       nv = 1.0f;
     }
     norms[row] = nv;
@@ -418,18 +418,8 @@ inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
 void launch_row_norms(const DevState &st, int row0, int nrows, cudaStream_t s) {
   if (nrows <= 0) return;
-  const int chunk = std::min(st.d, kNormChunk);
-  const size_t smem = (size_t)kNormRows * (chunk + 1) * sizeof(float);
-  static unsigned configured = 0u;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 32 && !(configured & (1u << dev))) {
-    cudaFuncSetAttribute(k_row_norms, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)((size_t)kNormRows * (kNormChunk + 1) * sizeof(float)));
-    configured |= (1u << dev);
-  }
-  k_row_norms<<<cdiv(nrows, kNormRows), 128, smem, s>>>(st.X, st.norms, st.snorms, st.ld, st.d,
-                                                        row0, nrows, st.cosine);
+  k_row_norms<<<cdiv(nrows, kNormRows), 256, 0, s>>>(st.X, st.norms, st.snorms, st.ld, st.d,
+                                                      row0, nrows, st.cosine);
   note_launch();
 }
 

@@ -463,34 +463,66 @@ __global__ void __launch_bounds__(kScanThreads)
   }
 }
 
-// Stages rows ra / rb (this lane's pair; dummies for idle lanes) 32 features
-// at a time and runs each lane's canonical chain.
-GM_D float warp_pair_dot(const float *X, int ld, int d, int ra, int rb,
-                         float (*ta)[kTileLd], float (*tb)[kTileLd]) {
+// 32 canonical chains per warp, one per lane (pair ra, rb; dummies for idle
+// lanes).  Feature chunks of 32 columns of the 64 rows are copied into a ring
+// of kRing shared-memory slots by 4-byte cp.async (each lane copies column
+// `lane` of every row: coalesced), kRing - 1 chunks ahead of the chain.
+constexpr int kRing = 4;
+constexpr int kPairWarps = 2;
+struct PairTiles {
+  float a[kRing][kTile][kTileLd];
+  float b[kRing][kTile][kTileLd];
+  int ra[kTile], rb[kTile];
+};
+constexpr size_t kPairSmem = sizeof(PairTiles) * kPairWarps;
+
+GM_D void cp_async4(float *dst, const float *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src)
+               : "memory");
+}
+GM_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+GM_D void cp_async_wait_ring() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(kRing - 1) : "memory");
+}
+
+GM_D float warp_pair_dot(const float *X, int ld, int d, int ra, int rb, PairTiles &t) {
   const int lane = threadIdx.x & 31;
-  float dot = 0.0f;
-  for (int i0 = 0; i0 < d; i0 += kTile) {
-    const int c = i0 + lane;
+  t.ra[lane] = ra;
+  t.rb[lane] = rb;
+  __syncwarp();
+  const int nch = (d + kTile - 1) / kTile;
+  // one commit group per chunk index (empty past the last chunk), so that
+  // "at most kRing - 1 groups pending" means chunk c has landed
+  auto issue = [&](int c) {
+    const int col = c * kTile + lane;
+    if (c < nch && col < d) {
+      const int slot = c % kRing;
 #pragma unroll 8
-    for (int r = 0; r < kTile; ++r) {
-      const int a = __shfl_sync(0xffffffffu, ra, r);
-      const int b = __shfl_sync(0xffffffffu, rb, r);
-      ta[r][lane] = c < d ? X[(size_t)a * ld + c] : 0.0f;
-      tb[r][lane] = c < d ? X[(size_t)b * ld + c] : 0.0f;
+      for (int r = 0; r < kTile; ++r) {
+        cp_async4(&t.a[slot][r][lane], X + (size_t)t.ra[r] * ld + col);
+        cp_async4(&t.b[slot][r][lane], X + (size_t)t.rb[r] * ld + col);
+      }
     }
+    cp_async_commit();
+  };
+  for (int c = 0; c < kRing - 1; ++c) issue(c);
+  float dot = 0.0f;
+  for (int c = 0; c < nch; ++c) {
+    issue(c + kRing - 1);  // refills the slot the previous iteration consumed
+    cp_async_wait_ring();
     __syncwarp();
-    const int lim = min(kTile, d - i0);
-    for (int i = 0; i < lim; ++i) dot = __fmaf_rn(ta[lane][i], tb[lane][i], dot);
+    const int slot = c % kRing, lim = min(kTile, d - c * kTile);
+    for (int i = 0; i < lim; ++i) dot = __fmaf_rn(t.a[slot][lane][i], t.b[slot][lane][i], dot);
     __syncwarp();
   }
   return dot;
 }
 
-constexpr int kPairWarps = 4;
 __global__ void __launch_bounds__(kPairWarps * 32)
     k_pair_dists(const float *X, int ld, int d, const float *norms, int brow0, const int *pool_j,
                  const int *pool_m, float *pool_d, const int *counter, long pool_cap) {
-  __shared__ float ta[kPairWarps][kTile][kTileLd], tb[kPairWarps][kTile][kTileLd];
+  extern __shared__ __align__(16) unsigned char pair_smem[];
+  PairTiles &t = reinterpret_cast<PairTiles *>(pair_smem)[threadIdx.x >> 5];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long total = min((long)*counter, pool_cap);
   const long nw = (long)gridDim.x * kPairWarps;
@@ -499,7 +531,7 @@ __global__ void __launch_bounds__(kPairWarps * 32)
     const bool ok = e < total;
     const int a = ok ? pool_j[e] : 0;
     const int b = ok ? brow0 + pool_m[e] : 0;
-    const float dot = warp_pair_dot(X, ld, d, a, b, ta[w], tb[w]);
+    const float dot = warp_pair_dot(X, ld, d, a, b, t);
     if (ok) pool_d[e] = canon_dist(norms[a], norms[b], dot);
   }
 }
@@ -507,7 +539,8 @@ __global__ void __launch_bounds__(kPairWarps * 32)
 __global__ void __launch_bounds__(kPairWarps * 32)
     k_row_dists(const float *X, int ld, int d, const float *norms, int brow0, const int *cand,
                 long cand_ld, const int *row_cnt, float *cand_d) {
-  __shared__ float ta[kPairWarps][kTile][kTileLd], tb[kPairWarps][kTile][kTileLd];
+  extern __shared__ __align__(16) unsigned char pair_smem[];
+  PairTiles &t = reinterpret_cast<PairTiles *>(pair_smem)[threadIdx.x >> 5];
   const int ml = blockIdx.x, row = brow0 + ml;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cnt = row_cnt[ml];
@@ -515,7 +548,7 @@ __global__ void __launch_bounds__(kPairWarps * 32)
   for (int g = w * 32; g < cnt; g += kPairWarps * 32) {
     const int c = g + lane;
     const int b = c < cnt ? cl[c] : row;
-    const float dot = warp_pair_dot(X, ld, d, row, b, ta[w], tb[w]);
+    const float dot = warp_pair_dot(X, ld, d, row, b, t);
     if (c < cnt) cand_d[(long)ml * cand_ld + c] = canon_dist(norms[row], norms[b], dot);
   }
 }
@@ -693,14 +726,24 @@ void launch_exact_screen(const DevState &st, int row0, int blk0, int nrows, int 
                                             coef, st.g_key, x.slab, x.pool_j, x.pool_m);
     note_launch(3);
   }
-  k_row_dists<<<nrows, kPairWarps * 32, 0, s>>>(st.X, st.ld, st.d, st.norms, brow0, x.cand, ldD,
-                                               x.row_cnt, x.cand_d);
+  static unsigned pair_configured = 0u;
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 32 && !(pair_configured & (1u << dev))) {
+      cudaFuncSetAttribute(k_row_dists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPairSmem);
+      cudaFuncSetAttribute(k_pair_dists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPairSmem);
+      pair_configured |= (1u << dev);
+    }
+  }
+  k_row_dists<<<nrows, kPairWarps * 32, kPairSmem, s>>>(st.X, st.ld, st.d, st.norms, brow0, x.cand,
+                                                       ldD, x.row_cnt, x.cand_d);
   note_launch();
   k_row_select<<<cdiv(nrows, kRowWarps), kRowWarps * 32, 0, s>>>(x.cand_d, brow0, nrows, x.cand,
                                                                  ldD, x.row_cnt, st.g_key);
   note_launch();
   if (row0 > 0) {
-    k_pair_dists<<<4 * std::max(sms, 1), kPairWarps * 32, 0, s>>>(
+    k_pair_dists<<<4 * std::max(sms, 1), kPairWarps * 32, kPairSmem, s>>>(
         st.X, st.ld, st.d, st.norms, brow0, x.pool_j, x.pool_m, x.pool_d, x.counter, x.pool_cap);
     note_launch();
     k_col_merge<<<cdiv(row0, kMergeWarps), kMergeWarps * 32, 0, s>>>(

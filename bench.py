@@ -67,6 +67,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-u2000", action="store_true")
     return ap.parse_args()
 
 
@@ -391,6 +392,18 @@ def main():
         line["exact_pairs_per_step"] = sum(s_.exact_pairs for s_ in stats) / args.steps
         line["exact_rescored_per_step"] = sum(s_.exact_rescored for s_ in stats) / args.steps
     line["clocks"] = clk.summary()
+
+    if args.precision == 1 and not args.no_u2000 and upd != UPD_OPS:
+        # the same exact insertion under the plain path's schedule (U = 2000
+        # NN-Descent update ops per cycle, which find nothing left to improve)
+        s, _, _, _, _ = step(1, UPD_OPS, False)
+        del s
+        flush_l2(flush)
+        s, ms1, _, rec1, rounds1 = step(1, UPD_OPS, False)
+        del s
+        line["schedule_u2000"] = {"value": n / (ms1 / 1000.0), "unit": "points/s", "recall_at_15": rec1,
+                                  "schedule": f"run_with_n_ops({CHUNK},{UPD_OPS},{emb})",
+                                  "final_update_cycles": rounds1}
 
     if args.precision == 1 and not args.no_plain:
         s, _, _, _, _ = step(0, UPD_OPS, False)

@@ -86,39 +86,48 @@ __global__ void k_mean_final(const float *part, const int *ipart, int nb, float 
 // sigma / rho per row, one warp per row; the bisection's target sum is
 // accumulated in FP64 by a fixed butterfly (reference smooth_knn_dist_kernel,
 // embedding_kernel.cuh:135-207).
+// sigma / rho by bisection (reference smooth_knn_dist).  A row occupies a
+// group of G lanes (G = 16 when k <= 16, two rows per warp, else 32).  The
+// target sum is accumulated in FP64 by an xor butterfly over the group; for
+// k <= 16 the upper 16 lanes of a 32-lane butterfly would only add exact
+// zeros, so the 16-lane butterfly gives the same bits with half the FP64
+// additions (FP64 is slow on this part).
+template <int G>
 __global__ void k_smooth_knn(const float *pub_dist, int n, int k, int euclid,
                              const float *fscal, double target, float *sigma,
                              float *rho) {
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (warp >= n) return;
-  const int row = warp;
-  const float raw = (lane < k) ? edist(pub_dist, k, row, lane, euclid) : 0.0f;
-  const float san = (lane < k && valid_d(raw)) ? raw : 0.0f;
+  const int gl = lane & (G - 1);          // lane within the row's group
+  const int base = lane - gl;             // first lane of the group
+  const long gid = ((long)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const bool live = gid < n;
+  const int row = live ? (int)gid : 0;
+  const float raw = (live && gl < k) ? edist(pub_dist, k, row, gl, euclid) : 0.0f;
+  const float san = (live && gl < k && valid_d(raw)) ? raw : 0.0f;
   float sum = 0.0f;
-  for (int c = 0; c < k; ++c) sum = __fadd_rn(sum, __shfl_sync(0xffffffffu, san, c));
-  const unsigned nz = __ballot_sync(0xffffffffu, lane < k && san > 0.0f);
+  for (int c = 0; c < k; ++c) sum = __fadd_rn(sum, __shfl_sync(0xffffffffu, san, base + c));
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (0xffffu << base);
+  const unsigned nz = __ballot_sync(0xffffffffu, gl < k && san > 0.0f) & gmask;
   const float mean_dist = fscal[FS_MEAN];
-  if (nz == 0u) {
-    if (lane == 0) {
-      rho[row] = 0.0f;
-      sigma[row] = __fmul_rn(kMinKDistScale, mean_dist);
-    }
-    return;
-  }
-  const int start_nz = __ffs(nz) - 1;
-  const float row_mean = __fdiv_rn(sum, (float)k);
+  const int start_nz = nz ? __ffs(nz) - 1 : base;
   const float r = __shfl_sync(0xffffffffu, raw, start_nz);
+  const float row_mean = __fdiv_rn(sum, (float)k);
   float lo = 0.0f, hi = FLT_MAX, mid = 1.0f;
-  const bool contrib = (lane >= 2 && lane < k);
+  const bool contrib = (gl >= 2 && gl < k);
   const float dj = __fsub_rn(san, r);
+  bool done = !live || nz == 0u;
   for (int it = 0; it < 64; ++it) {
+    if (__all_sync(0xffffffffu, done)) break;
     double term = 0.0;
-    if (contrib) term = (dj > 0.0f) ? (double)gm_expf(__fdiv_rn(-dj, mid)) : 1.0;
+    if (contrib && !done) term = (dj > 0.0f) ? (double)gm_expf(__fdiv_rn(-dj, mid)) : 1.0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
+    for (int o = G / 2; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
+    if (done) continue;
     const double psum = term;
-    if (fabs(psum - target) < (double)kSmoothTol) break;
+    if (fabs(psum - target) < (double)kSmoothTol) {
+      done = true;
+      continue;
+    }
     if (psum > target) {
       hi = mid;
       mid = __fmul_rn(__fadd_rn(lo, hi), 0.5f);
@@ -127,12 +136,16 @@ __global__ void k_smooth_knn(const float *pub_dist, int n, int k, int euclid,
       mid = (hi == FLT_MAX) ? __fmul_rn(mid, 2.0f) : __fmul_rn(__fadd_rn(lo, hi), 0.5f);
     }
   }
+  if (!live || gl != 0) return;
+  if (nz == 0u) {
+    rho[row] = 0.0f;
+    sigma[row] = __fmul_rn(kMinKDistScale, mean_dist);
+    return;
+  }
   if (!isfinite(mid) || mid <= 0.0f) mid = 1.0f;
   const float min_scale = __fmul_rn(kMinKDistScale, (r > 0.0f) ? row_mean : mean_dist);
-  if (lane == 0) {
-    rho[row] = r;
-    sigma[row] = mid < min_scale ? min_scale : mid;
-  }
+  rho[row] = r;
+  sigma[row] = mid < min_scale ? min_scale : mid;
 }
 
 // Directed membership p_ij for batch rows and the fuzzy union
@@ -676,8 +689,12 @@ void launch_fuzzy_graph(const uint32_t *pub_idx, const float *pub_dist, int n, i
   note_launch();
   k_mean_final<<<1, 1, 0, s>>>(e.partial, e.ipartial, nbl, e.fscal);
   note_launch();
-  k_smooth_knn<<<cdiv((long)n * 32, 256), 256, 0, s>>>(pub_dist, n, k, euclidean, e.fscal,
-                                                       log2_target, e.sigma, e.rho);
+  if (k <= 16)
+    k_smooth_knn<16><<<cdiv((long)n * 16, 256), 256, 0, s>>>(pub_dist, n, k, euclidean, e.fscal,
+                                                             log2_target, e.sigma, e.rho);
+  else
+    k_smooth_knn<32><<<cdiv((long)n * 32, 256), 256, 0, s>>>(pub_dist, n, k, euclidean, e.fscal,
+                                                             log2_target, e.sigma, e.rho);
   note_launch();
   const int ndir = nb * k;
   if (ndir > 0)

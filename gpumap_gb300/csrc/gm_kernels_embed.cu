@@ -363,9 +363,12 @@ GM_D void sgd_edge(float *emb, int row, int j, int kk, float ep, float &ns, floa
       const float ex = __fsub_rn(cur0, q0), ey = __fsub_rn(cur1, q1);
       const float d2n = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
       float rep = 0.0f;
+      // repulsion: d2n^b by the hardware exp2 / log2 (__powf); these sampled
+      // Hogwild updates are compared statistically, and the attraction
+      // above keeps the series pow
       if (d2n > 0.0f)
         rep = __fdiv_rn(two_gb, __fmul_rn(__fadd_rn(0.001f, d2n),
-                                          __fadd_rn(__fmul_rn(a, gm_powf(d2n, b)), 1.0f)));
+                                          __fadd_rn(__fmul_rn(a, __powf(d2n, b)), 1.0f)));
       const float h0 = (rep > 0.0f) ? __fmul_rn(fclip(__fmul_rn(rep, ex)), alpha) : a4;
       const float h1 = (rep > 0.0f) ? __fmul_rn(fclip(__fmul_rn(rep, ey)), alpha) : a4;
       cur0 = __fadd_rn(cur0, h0);

@@ -38,9 +38,11 @@ constexpr int kABytes = kTM * kTK * 2;         // 16 KB
 constexpr int kBBytes = kTN * kTK * 2;         // 32 KB
 constexpr int kStageBytes = kABytes + kBBytes; // 48 KB
 constexpr int kExactThreads = 192;             // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
-constexpr int kTmemCols = 256;                 // one 128 x 256 FP32 accumulator
+constexpr int kTmemCols = 512;                 // two 128 x 256 FP32 accumulators
 constexpr uint32_t kWaitLimit = 1u << 24;      // bounded mbarrier waits
-constexpr size_t kExactSmem = (size_t)kStages * kStageBytes + 1024 + 256;
+constexpr int kStagePitch = 33;                // epilogue staging row pitch (floats)
+constexpr size_t kEpiBytes = (size_t)4 * 32 * kStagePitch * sizeof(float);
+constexpr size_t kExactSmem = (size_t)kStages * kStageBytes + 1024 + 256 + kEpiBytes;
 
 // Instruction descriptor, kind::f16: D=F32 (bits 4-5), A=B=BF16 (7-9, 10-12),
 // both K-major (15, 16 = 0), N>>3 at 17-22, M>>4 at 24-28.
@@ -153,9 +155,10 @@ __global__ void __launch_bounds__(kExactThreads, 1)
   unsigned char *base = (unsigned char *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(base + (size_t)kStages * kStageBytes);
   uint64_t *empty = full + kStages;
-  uint64_t *tmem_full = empty + kStages;
-  uint64_t *tmem_empty = tmem_full + 1;
-  uint32_t *tmem_slot = (uint32_t *)(tmem_empty + 1);
+  uint64_t *tmem_full = empty + kStages;  // [2]: accumulator b holds a finished tile
+  uint64_t *tmem_empty = tmem_full + 2;   // [2]: accumulator b has been drained
+  uint32_t *tmem_slot = (uint32_t *)(tmem_empty + 2);
+  float *epi = (float *)(base + (size_t)kStages * kStageBytes + 256);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int mt = blockIdx.y;
@@ -167,8 +170,10 @@ __global__ void __launch_bounds__(kExactThreads, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(tmem_full, 1);
-    mbar_init(tmem_empty, 128);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tmem_full[b], 1);
+      mbar_init(&tmem_empty[b], 128);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -205,65 +210,78 @@ __global__ void __launch_bounds__(kExactThreads, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
+      // tile tc accumulates in TMEM columns [256 (tc & 1), +256): the MMAs of
+      // the next tile run while the epilogue drains this one
       uint32_t it = 0, tc = 0;
       for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x, ++tc) {
-        if (tc > 0 && !mbar_wait(tmem_empty, (tc - 1) & 1)) {
+        const uint32_t b = tc & 1u, use = tc >> 1;
+        if (use > 0 && !mbar_wait(&tmem_empty[b], (use - 1) & 1)) {
           ok = false;
           break;
         }
         tc_fence_after();
+        const uint32_t acc = tmem + b * (uint32_t)kTN;
         for (int kc = 0; kc < 3 * kchunks; ++kc, ++it) {
-          const uint32_t s = it % kStages, use = it / kStages;
-          if (!mbar_wait(&full[s], use & 1)) {
+          const uint32_t s = it % kStages, u2 = it / kStages;
+          if (!mbar_wait(&full[s], u2 & 1)) {
             ok = false;
             break;
           }
           tc_fence_after();
           const uint32_t a = smem_u32(base + (size_t)s * kStageBytes);
-          const uint32_t b = a + kABytes;
+          const uint32_t bb = a + kABytes;
 #pragma unroll
           for (int k = 0; k < kTK / 16; ++k)
-            umma_bf16(tmem, sw128_desc(a + k * 32), sw128_desc(b + k * 32),
+            umma_bf16(acc, sw128_desc(a + k * 32), sw128_desc(bb + k * 32),
                       (kc | k) != 0 ? 1u : 0u);
           umma_commit(&empty[s]);
         }
         if (!ok) break;
-        umma_commit(tmem_full);
+        umma_commit(&tmem_full[b]);
       }
       if (!ok) atomicOr(err, kDevErrSpin);
     }
     __syncwarp();
   } else {
-    // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (tile rows)
+    // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (tile rows); each
+    // 32 x 32 chunk is staged in shared memory (pitch 33: conflict free) and
+    // written out a row segment (128 contiguous bytes) per store
     const int quarter = warp & 3;
     const int r = quarter * 32 + lane;
     const int m = m0 + r;
-    const bool row_ok = m < nb;
-    const float nm = row_ok ? norms[arow0 + m] : 0.0f;
+    const float nm = m < nb ? norms[arow0 + m] : 0.0f;
+    float *stg = epi + (size_t)quarter * 32 * kStagePitch;
     uint32_t tc = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++tc) {
-      if (!mbar_wait(tmem_full, tc & 1)) {
+      const uint32_t b = tc & 1u;
+      if (!mbar_wait(&tmem_full[b], (tc >> 1) & 1)) {
         if (lane == 0) atomicOr(err, kDevErrSpin);
         break;
       }
       tc_fence_after();
       for (int c = 0; c < kTN; c += 32) {
         uint32_t v[32];
-        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c, v);
+        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + b * (uint32_t)kTN + (uint32_t)c, v);
         const int col0 = t * kTN + c;
-        if (row_ok) {
-          float *out = D + (long)m * ldD + col0;
+        const float njl = col0 + lane < n ? norms[col0 + lane] : 0.0f;
 #pragma unroll
-          for (int i = 0; i < 32; ++i) {
-            const int j = col0 + i;
-            if (j < n)
-              out[i] = __fsub_rn(__fadd_rn(nm, norms[j]),
-                                 __fmul_rn(2.0f, __uint_as_float(v[i])));
+        for (int i = 0; i < 32; ++i) {
+          const float nj = __shfl_sync(0xffffffffu, njl, i);
+          stg[lane * kStagePitch + i] =
+              __fsub_rn(__fadd_rn(nm, nj), __fmul_rn(2.0f, __uint_as_float(v[i])));
+        }
+        __syncwarp();
+        if (col0 + lane < n) {
+#pragma unroll 4
+          for (int rr = 0; rr < 32; ++rr) {
+            const int mrow = m0 + quarter * 32 + rr;
+            if (mrow < nb) D[(long)mrow * ldD + col0 + lane] = stg[rr * kStagePitch + lane];
           }
         }
+        __syncwarp();
       }
       tc_fence_before();
-      mbar_arrive(tmem_empty);
+      mbar_arrive(&tmem_empty[b]);
     }
   }
   tc_fence_before();

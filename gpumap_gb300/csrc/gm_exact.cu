@@ -554,20 +554,55 @@ __global__ void __launch_bounds__(kPairWarps * 32)
   }
 }
 
-__global__ void __launch_bounds__(kPairWarps * 32)
+// Row candidates: the batch row is common to the warp, so only the candidate
+// rows go through the ring; lane l holds feature c0 + l of the batch row and
+// hands it to every chain by a shuffle.
+constexpr int kRowDistWarps = 4;
+struct RowTiles {
+  float b[kRing][kTile][kTileLd];
+  float a[kRing][kTile];
+  int rb[kTile];
+};
+constexpr size_t kRowSmem = sizeof(RowTiles) * kRowDistWarps;
+
+__global__ void __launch_bounds__(kRowDistWarps * 32)
     k_row_dists(const float *X, int ld, int d, const float *norms, int brow0, const int *cand,
                 long cand_ld, const int *row_cnt, float *cand_d) {
-  extern __shared__ __align__(16) unsigned char pair_smem[];
-  PairTiles &t = reinterpret_cast<PairTiles *>(pair_smem)[threadIdx.x >> 5];
+  extern __shared__ __align__(16) unsigned char row_smem[];
+  RowTiles &t = reinterpret_cast<RowTiles *>(row_smem)[threadIdx.x >> 5];
   const int ml = blockIdx.x, row = brow0 + ml;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cnt = row_cnt[ml];
   const int *cl = cand + (long)ml * cand_ld;
-  for (int g = w * 32; g < cnt; g += kPairWarps * 32) {
+  const float *xa = X + (size_t)row * ld;
+  const int nch = (d + kTile - 1) / kTile;
+  for (int g = w * 32; g < cnt; g += kRowDistWarps * 32) {
     const int c = g + lane;
-    const int b = c < cnt ? cl[c] : row;
-    const float dot = warp_pair_dot(X, ld, d, row, b, t);
-    if (c < cnt) cand_d[(long)ml * cand_ld + c] = canon_dist(norms[row], norms[b], dot);
+    t.rb[lane] = c < cnt ? cl[c] : row;
+    __syncwarp();
+    auto issue = [&](int ch) {
+      const int col = ch * kTile + lane;
+      if (ch < nch && col < d) {
+        const int slot = ch % kRing;
+        cp_async4(&t.a[slot][lane], xa + col);
+#pragma unroll 8
+        for (int r = 0; r < kTile; ++r)
+          cp_async4(&t.b[slot][r][lane], X + (size_t)t.rb[r] * ld + col);
+      }
+      cp_async_commit();
+    };
+    for (int ch = 0; ch < kRing - 1; ++ch) issue(ch);
+    float dot = 0.0f;
+    for (int ch = 0; ch < nch; ++ch) {
+      issue(ch + kRing - 1);
+      cp_async_wait_ring();
+      __syncwarp();
+      const int slot = ch % kRing, lim = min(kTile, d - ch * kTile);
+      for (int i = 0; i < lim; ++i) dot = __fmaf_rn(t.a[slot][i], t.b[slot][lane][i], dot);
+      __syncwarp();
+    }
+    if (c < cnt) cand_d[(long)ml * cand_ld + c] = canon_dist(norms[row], norms[t.rb[lane]], dot);
+    __syncwarp();
   }
 }
 
@@ -749,13 +784,13 @@ void launch_exact_screen(const DevState &st, int row0, int blk0, int nrows, int 
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 32 && !(pair_configured & (1u << dev))) {
-      cudaFuncSetAttribute(k_row_dists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPairSmem);
+      cudaFuncSetAttribute(k_row_dists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRowSmem);
       cudaFuncSetAttribute(k_pair_dists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPairSmem);
       pair_configured |= (1u << dev);
     }
   }
-  k_row_dists<<<nrows, kPairWarps * 32, kPairSmem, s>>>(st.X, st.ld, st.d, st.norms, brow0, x.cand,
-                                                       ldD, x.row_cnt, x.cand_d);
+  k_row_dists<<<nrows, kRowDistWarps * 32, kRowSmem, s>>>(st.X, st.ld, st.d, st.norms, brow0,
+                                                         x.cand, ldD, x.row_cnt, x.cand_d);
   note_launch();
   k_row_select<<<cdiv(nrows, kRowWarps), kRowWarps * 32, 0, s>>>(x.cand_d, brow0, nrows, x.cand,
                                                                  ldD, x.row_cnt, st.g_key);

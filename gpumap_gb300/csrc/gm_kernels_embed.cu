@@ -73,14 +73,30 @@ __global__ void k_mean_partial(const float *pub_dist, int n, int k, int euclid,
   }
 }
 
+// Ordered sum of the partials: a block stages them in shared memory by
+// coalesced loads, then thread 0 adds them in index order.
+constexpr int kMeanStage = 4096;
 __global__ void k_mean_final(const float *part, const int *ipart, int nb, float *fscal) {
+  __shared__ float sp[kMeanStage];
+  __shared__ int si[kMeanStage];
   float s = 0.0f;
   long c = 0;
-  for (int i = 0; i < nb; ++i) {
-    s = __fadd_rn(s, part[i]);
-    c += ipart[i];
+  for (int i0 = 0; i0 < nb; i0 += kMeanStage) {
+    const int m = min(kMeanStage, nb - i0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      sp[i] = part[i0 + i];
+      si[i] = ipart[i0 + i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int i = 0; i < m; ++i) {
+        s = __fadd_rn(s, sp[i]);
+        c += si[i];
+      }
   }
-  fscal[FS_MEAN] = (c > 0 && isfinite(s) && s > 0.0f) ? __fdiv_rn(s, (float)c) : 1.0f;
+  if (threadIdx.x == 0)
+    fscal[FS_MEAN] = (c > 0 && isfinite(s) && s > 0.0f) ? __fdiv_rn(s, (float)c) : 1.0f;
 }
 
 // sigma / rho per row, one warp per row; the bisection's target sum is
@@ -690,7 +706,7 @@ void launch_fuzzy_graph(const uint32_t *pub_idx, const float *pub_dist, int n, i
   const int nbl = cdiv(total, 256);
   k_mean_partial<<<nbl, 256, 0, s>>>(pub_dist, n, k, euclidean, e.partial, e.ipartial);
   note_launch();
-  k_mean_final<<<1, 1, 0, s>>>(e.partial, e.ipartial, nbl, e.fscal);
+  k_mean_final<<<1, 256, 0, s>>>(e.partial, e.ipartial, nbl, e.fscal);
   note_launch();
   if (k <= 16)
     k_smooth_knn<16><<<cdiv((long)n * 16, 256), 256, 0, s>>>(pub_dist, n, k, euclidean, e.fscal,

@@ -479,8 +479,7 @@ GM_D unsigned ld_acquire(const unsigned *p) {
 GM_D void grid_arrive(unsigned *count) {
   __syncthreads();
   if (threadIdx.x == 0)
-    asm volatile("fence.acq_rel.gpu;\n\tred.relaxed.gpu.global.add.u32 [%0], 1;" ::"l"(count)
-                 : "memory");
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(count) : "memory");
 }
 // Wait until every CTA has arrived (count >= target); bounded.
 GM_D bool grid_wait(unsigned *count, unsigned target, unsigned *err) {

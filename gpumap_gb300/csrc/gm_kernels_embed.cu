@@ -102,49 +102,42 @@ __global__ void k_mean_final(const float *part, const int *ipart, int nb, float 
 // sigma / rho per row, one warp per row; the bisection's target sum is
 // accumulated in FP64 by a fixed butterfly (reference smooth_knn_dist_kernel,
 // embedding_kernel.cuh:135-207).
-// sigma / rho by bisection (reference smooth_knn_dist).  A row occupies a
-// group of G lanes (G = 16 when k <= 16, two rows per warp, else 32).  The
-// target sum is accumulated in FP64 by an xor butterfly over the group; for
-// k <= 16 the upper 16 lanes of a 32-lane butterfly would only add exact
-// zeros, so the 16-lane butterfly gives the same bits with half the FP64
-// additions (FP64 is slow on this part).
-template <int G>
+// sigma / rho by bisection (reference smooth_knn_dist, one warp per row for
+// k > 16).  The bisection's target sum is accumulated in FP64 by the fixed
+// xor-butterfly order of 32 lanes, term c on lane c (the terms of lanes >= k
+// are +0, adding them is exact).
 __global__ void k_smooth_knn(const float *pub_dist, int n, int k, int euclid,
                              const float *fscal, double target, float *sigma,
                              float *rho) {
   const int lane = threadIdx.x & 31;
-  const int gl = lane & (G - 1);          // lane within the row's group
-  const int base = lane - gl;             // first lane of the group
-  const long gid = ((long)blockIdx.x * blockDim.x + threadIdx.x) / G;
-  const bool live = gid < n;
-  const int row = live ? (int)gid : 0;
-  const float raw = (live && gl < k) ? edist(pub_dist, k, row, gl, euclid) : 0.0f;
-  const float san = (live && gl < k && valid_d(raw)) ? raw : 0.0f;
+  const long gid = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (gid >= n) return;
+  const int row = (int)gid;
+  const float raw = lane < k ? edist(pub_dist, k, row, lane, euclid) : 0.0f;
+  const float san = (lane < k && valid_d(raw)) ? raw : 0.0f;
   float sum = 0.0f;
-  for (int c = 0; c < k; ++c) sum = __fadd_rn(sum, __shfl_sync(0xffffffffu, san, base + c));
-  const unsigned gmask = (G == 32) ? 0xffffffffu : (0xffffu << base);
-  const unsigned nz = __ballot_sync(0xffffffffu, gl < k && san > 0.0f) & gmask;
+  for (int c = 0; c < k; ++c) sum = __fadd_rn(sum, __shfl_sync(0xffffffffu, san, c));
+  const unsigned nz = __ballot_sync(0xffffffffu, lane < k && san > 0.0f);
   const float mean_dist = fscal[FS_MEAN];
-  const int start_nz = nz ? __ffs(nz) - 1 : base;
-  const float r = __shfl_sync(0xffffffffu, raw, start_nz);
+  if (nz == 0u) {
+    if (lane == 0) {
+      rho[row] = 0.0f;
+      sigma[row] = __fmul_rn(kMinKDistScale, mean_dist);
+    }
+    return;
+  }
+  const float r = __shfl_sync(0xffffffffu, raw, __ffs(nz) - 1);
   const float row_mean = __fdiv_rn(sum, (float)k);
   float lo = 0.0f, hi = FLT_MAX, mid = 1.0f;
-  const bool contrib = (gl >= 2 && gl < k);
+  const bool contrib = lane >= 2 && lane < k;
   const float dj = __fsub_rn(san, r);
-  bool done = !live || nz == 0u;
   for (int it = 0; it < 64; ++it) {
-    if (__all_sync(0xffffffffu, done)) break;
     double term = 0.0;
-    if (contrib && !done) term = (dj > 0.0f) ? (double)gm_expf(__fdiv_rn(-dj, mid)) : 1.0;
+    if (contrib) term = (dj > 0.0f) ? (double)gm_expf(__fdiv_rn(-dj, mid)) : 1.0;
 #pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
-    if (done) continue;
-    const double psum = term;
-    if (fabs(psum - target) < (double)kSmoothTol) {
-      done = true;
-      continue;
-    }
-    if (psum > target) {
+    for (int o = 16; o > 0; o >>= 1) term += __shfl_xor_sync(0xffffffffu, term, o);
+    if (fabs(term - target) < (double)kSmoothTol) break;
+    if (term > target) {
       hi = mid;
       mid = __fmul_rn(__fadd_rn(lo, hi), 0.5f);
     } else {
@@ -152,8 +145,90 @@ __global__ void k_smooth_knn(const float *pub_dist, int n, int k, int euclid,
       mid = (hi == FLT_MAX) ? __fmul_rn(mid, 2.0f) : __fmul_rn(__fadd_rn(lo, hi), 0.5f);
     }
   }
-  if (!live || gl != 0) return;
-  if (nz == 0u) {
+  if (lane != 0) return;
+  if (!isfinite(mid) || mid <= 0.0f) mid = 1.0f;
+  const float min_scale = __fmul_rn(kMinKDistScale, (r > 0.0f) ? row_mean : mean_dist);
+  rho[row] = r;
+  sigma[row] = mid < min_scale ? min_scale : mid;
+}
+
+// The same for k <= 16 with four lanes per row (eight rows per warp).  Lane
+// q of a row holds terms c = q, q+4, q+8, q+12 and forms
+// (t[q] + t[q+8]) + (t[q+4] + t[q+12]); two more xor steps over the four
+// lanes finish the sum.  For k <= 16 this is exactly the 32-lane butterfly's
+// tree (its first step only adds the exact zeros of lanes 16-31, the next two
+// are these per-lane additions), so every bit agrees with the warp-per-row
+// form, with a quarter of the FP64 additions (FP64 is slow on this part).
+__global__ void k_smooth_knn4(const float *pub_dist, int n, int k, int euclid,
+                              const float *fscal, double target, float *sigma,
+                              float *rho) {
+  const int lane = threadIdx.x & 31;
+  const int q = lane & 3, base = lane - q;
+  const long gid = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const bool live = gid < n;
+  const int row = live ? (int)gid : 0;
+  float raw[4], san[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = q + 4 * j;
+    raw[j] = (live && c < k) ? edist(pub_dist, k, row, c, euclid) : 0.0f;
+    san[j] = (live && c < k && valid_d(raw[j])) ? raw[j] : 0.0f;
+  }
+  // row sum in column order, first nonzero column
+  float sum = 0.0f;
+  int first = 64;
+#pragma unroll
+  for (int c = 0; c < 16; ++c) {
+    const float v = __shfl_sync(0xffffffffu, san[c >> 2], base + (c & 3));
+    if (c < k) {
+      sum = __fadd_rn(sum, v);
+      if (first == 64 && v > 0.0f) first = c;
+    }
+  }
+  const float mean_dist = fscal[FS_MEAN];
+  float r = 0.0f;
+#pragma unroll
+  for (int c = 0; c < 16; ++c) {
+    const float v = __shfl_sync(0xffffffffu, raw[c >> 2], base + (c & 3));
+    if (c == first) r = v;
+  }
+  const float row_mean = __fdiv_rn(sum, (float)k);
+  float lo = 0.0f, hi = FLT_MAX, mid = 1.0f;
+  float dj[4];
+  bool contrib[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = q + 4 * j;
+    contrib[j] = c >= 2 && c < k;
+    dj[j] = __fsub_rn(san[j], r);
+  }
+  bool done = !live || first == 64;
+  for (int it = 0; it < 64; ++it) {
+    if (__all_sync(0xffffffffu, done)) break;
+    double t[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      t[j] = 0.0;
+      if (contrib[j] && !done) t[j] = (dj[j] > 0.0f) ? (double)gm_expf(__fdiv_rn(-dj[j], mid)) : 1.0;
+    }
+    double term = (t[0] + t[2]) + (t[1] + t[3]);
+    term += __shfl_xor_sync(0xffffffffu, term, 2);
+    term += __shfl_xor_sync(0xffffffffu, term, 1);
+    if (done) continue;
+    if (fabs(term - target) < (double)kSmoothTol) {
+      done = true;
+      continue;
+    }
+    if (term > target) {
+      hi = mid;
+      mid = __fmul_rn(__fadd_rn(lo, hi), 0.5f);
+    } else {
+      lo = mid;
+      mid = (hi == FLT_MAX) ? __fmul_rn(mid, 2.0f) : __fmul_rn(__fadd_rn(lo, hi), 0.5f);
+    }
+  }
+  if (!live || q != 0) return;
+  if (first == 64) {
     rho[row] = 0.0f;
     sigma[row] = __fmul_rn(kMinKDistScale, mean_dist);
     return;
@@ -708,11 +783,11 @@ void launch_fuzzy_graph(const uint32_t *pub_idx, const float *pub_dist, int n, i
   k_mean_final<<<1, 256, 0, s>>>(e.partial, e.ipartial, nbl, e.fscal);
   note_launch();
   if (k <= 16)
-    k_smooth_knn<16><<<cdiv((long)n * 16, 256), 256, 0, s>>>(pub_dist, n, k, euclidean, e.fscal,
-                                                             log2_target, e.sigma, e.rho);
+    k_smooth_knn4<<<cdiv((long)n * 4, 256), 256, 0, s>>>(pub_dist, n, k, euclidean, e.fscal,
+                                                         log2_target, e.sigma, e.rho);
   else
-    k_smooth_knn<32><<<cdiv((long)n * 32, 256), 256, 0, s>>>(pub_dist, n, k, euclidean, e.fscal,
-                                                             log2_target, e.sigma, e.rho);
+    k_smooth_knn<<<cdiv((long)n * 32, 256), 256, 0, s>>>(pub_dist, n, k, euclidean, e.fscal,
+                                                         log2_target, e.sigma, e.rho);
   note_launch();
   const int ndir = nb * k;
   if (ndir > 0)

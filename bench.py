@@ -256,6 +256,19 @@ def cpu_baseline_sample(X, upd, emb, cycles=2):
     return n / dt, dt, n
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
+# ncu captures of the 30,000-point cut of this workload (cycle 41: 20,500
+# columns), profiles/traffic_exact_30k_x784.md.  "per" names the unit the
+# traffic scales with, so that a capture can be carried to this run's mean
+# launch: k_exact_dist reads its B operand once per launch (bytes ~ FLOPs);
+# the SGD launch's traffic is the first touch of its edge arrays (about the
+# same per embedding call at any size, so it is used as measured).
+NCU_TRAFFIC = {
+    "k_exact_dist": {"bytes": 69587968 + 5130496, "per": "flop", "units": 6 * 500 * 20500 * 832},
+    "k_sgd_persistent": {"bytes": 871680 + 80128, "per": "launch", "units": 1},
+}
+
+
 def roofline(stats, d, peaks):
     """Per-kernel achieved rates; returns (dominant name, dict of all)."""
     hbm = peaks.get("hbm_gbs", 6800.0)
@@ -282,8 +295,16 @@ def roofline(stats, d, peaks):
         st["exact_launches"], "hbm")
     add("k_local_join", st["join_ms"], st["join_rows"] * d * 4 + st["join_pairs"] * 8, st["join_launches"], "hbm")
     add("k_candidate_dists", st["cand_ms"], st["cand_rows"] * d * 4, st["cand_launches"], "hbm")
-    add("k_sgd_epoch (200 per launch)", st["sgd_ms"], st["sgd_edges"] * 28 + (st["sgd_edges"] + st["sgd_negatives"]) * 8,
+    add("k_sgd_persistent", st["sgd_ms"], st["sgd_edges"] * 28 + (st["sgd_edges"] + st["sgd_negatives"]) * 8,
         st["sgd_launches"], "hbm")
+    for name, t in NCU_TRAFFIC.items():
+        if name not in agg:
+            continue
+        if t["per"] == "flop":
+            per_launch = st["exact_flops"] / max(st["exact_launches"], 1)
+            agg[name]["traffic"] = t["bytes"] * per_launch / t["units"]
+        else:
+            agg[name]["traffic"] = float(t["bytes"])
     dom = max(agg, key=lambda k: agg[k]["ms"]) if agg else None
     return dom, agg
 
@@ -375,7 +396,7 @@ def main():
     roof = dict(kernels[dom]) if dom else {}
     if dom:
         roof = {"kernel": dom, "bound": roof["bound"], "achieved": roof["achieved"], "peak": roof["peak"],
-                "unit": roof["unit"], "frac": roof["frac"], "traffic": None,
+                "unit": roof["unit"], "frac": roof["frac"], "traffic": roof.get("traffic"),
                 "peak_source": "measured (MEASURED_PEAKS.json, sustained bf16 / hbm copy)"}
     line = {
         "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,

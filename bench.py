@@ -257,15 +257,16 @@ def cpu_baseline_sample(X, upd, emb, cycles=2):
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
-# ncu captures of the 30,000-point cut of this workload (cycle 41: 20,500
-# columns), profiles/traffic_exact_30k_x784.md.  "per" names the unit the
+# ncu captures of the 30,000-point cut of this workload (k_exact_dist: cycle
+# 41, 20,500 columns, profiles/k_exact_dist_30k_x784.md; k_sgd_persistent:
+# cycle 40, profiles/k_sgd_persistent_30k_x784.md).  "per" names the unit the
 # traffic scales with, so that a capture can be carried to this run's mean
 # launch: k_exact_dist reads its B operand once per launch (bytes ~ FLOPs);
 # the SGD launch's traffic is the first touch of its edge arrays (about the
 # same per embedding call at any size, so it is used as measured).
 NCU_TRAFFIC = {
     "k_exact_dist": {"bytes": 69587968 + 5130496, "per": "flop", "units": 6 * 500 * 20500 * 832},
-    "k_sgd_persistent": {"bytes": 871680 + 80128, "per": "launch", "units": 1},
+    "k_sgd_persistent": {"bytes": 864512 + 79104, "per": "launch", "units": 1},
 }
 
 

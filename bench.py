@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--overlap", type=int, default=1, choices=[0, 1],
+                    help="run each cycle's embedding beside the next cycle's distance work")
     ap.add_argument("--update-ops", type=int, default=None,
                     help="U per cycle (default 0 for precision 1, 2000 for precision 0)")
     ap.add_argument("--embedding-ops", type=int, default=EMB_OPS)
@@ -170,11 +172,11 @@ def flush_l2(buf):
     buf.zero_()
 
 
-def run_value_step(native, X_dev, n, d, upd, emb, max_final, stats_on, q_idx, exact, precision):
+def run_value_step(native, X_dev, n, d, upd, emb, max_final, stats_on, q_idx, exact, precision, overlap=0):
     import torch
 
     p = native.default_params(n_instances=n, n_features=d, n_neighbors=K, max_epoch=MAX_EPOCH,
-                              device=torch.cuda.current_device(), precision=precision)
+                              device=torch.cuda.current_device(), precision=precision, overlap=overlap)
     p.a, p.b = 1.5769434602697652, 0.8950608778515733  # find_ab_params(1.0, 0.1)
     s = native.Session(p)
     s.set_stats(stats_on)
@@ -199,6 +201,7 @@ def run_value_step(native, X_dev, n, d, upd, emb, max_final, stats_on, q_idx, ex
         s.run(0, n, 0)
         rounds += 1
         rec = recall(table[q_dev, :K].cpu().numpy(), exact)
+    s.view("embedding")  # waits for the last embedding (overlap mode)
     end.record()
     torch.cuda.synchronize()
     ms = start.elapsed_time(end)
@@ -212,7 +215,7 @@ class _Cai:
                                          "strides": (cols * esz, esz), "data": (ptr, False)}
 
 
-def run_e2e_step(X_host, n, d, upd, emb, max_final, q_idx, exact, precision):
+def run_e2e_step(X_host, n, d, upd, emb, max_final, q_idx, exact, precision, overlap=0):
     import torch
 
     import gpumap_gb300 as gm
@@ -224,6 +227,7 @@ def run_e2e_step(X_host, n, d, upd, emb, max_final, q_idx, exact, precision):
     params.n_instances, params.n_features, params.n_neighbors = n, d, K
     params.max_epoch = MAX_EPOCH
     params.precision = precision
+    params.overlap = overlap
     model = gm.GPUMAP(ArrayDataLoader(X_host), params)
     for c in range(0, n, CHUNK):
         model.run_with_n_ops(min(CHUNK, n - c), upd, emb)
@@ -235,6 +239,7 @@ def run_e2e_step(X_host, n, d, upd, emb, max_final, q_idx, exact, precision):
         rounds += 1
         idx = model.get_neighbor_indices().cpu().numpy()
         rec = recall(idx[q_idx], exact)
+    model.get_embedding()  # waits for the last embedding (overlap mode)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     model.close()
@@ -323,7 +328,8 @@ def main():
                           f"run_with_n_ops({CHUNK},{upd},{emb}) per cycle, then "
                           f"run_with_n_ops(0,{n},0) until recall@15>={RECALL_TARGET}",
               "n_points": n, "n_features": d, "n_neighbors": K, "max_epoch": MAX_EPOCH,
-              "precision": args.precision, "update_ops": upd, "embedding_ops": emb,
+              "precision": args.precision, "overlap": args.overlap, "update_ops": upd,
+              "embedding_ops": emb,
               "l2": "inputs (220 MB) larger than L2; 512 MB flush between steps",
               "parallelism": "replicas" if world > 1 else "single GPU"}
 
@@ -367,9 +373,9 @@ def main():
     q_idx = np.random.default_rng(123).choice(n, min(RECALL_QUERIES, n), replace=False)
     exact = exact_knn_gpu(X_dev, q_idx, K)
 
-    def step(precision, u, stats_on):
+    def step(precision, u, stats_on, overlap=args.overlap):
         return run_value_step(native, X_dev, n, d, u, emb, args.max_final_updates, stats_on, q_idx, exact,
-                              precision)
+                              precision, overlap)
 
     for _ in range(args.warmup):
         s, _, _, _, _ = step(args.precision, upd, False)
@@ -416,6 +422,16 @@ def main():
         line["exact_rescored_per_step"] = sum(s_.exact_rescored for s_ in stats) / args.steps
     line["clocks"] = clk.summary()
 
+    if args.overlap:
+        # the same build with the phases one after another (the reference's
+        # order of work on the device)
+        s, _, _, _, _ = step(args.precision, upd, False, overlap=0)
+        del s
+        flush_l2(flush)
+        s, ms_s, _, rec_s, _ = step(args.precision, upd, False, overlap=0)
+        del s
+        line["value_no_overlap"] = {"value": n / (ms_s / 1000.0), "unit": "points/s", "recall_at_15": rec_s}
+
     if args.precision == 1 and not args.no_u2000 and upd != UPD_OPS:
         # the same exact insertion under the plain path's schedule (U = 2000
         # NN-Descent update ops per cycle, which find nothing left to improve)
@@ -443,11 +459,12 @@ def main():
 
     if not args.no_e2e:
         X_pin = torch.from_numpy(X).pin_memory().numpy()
-        run_e2e_step(X_pin, n, d, upd, emb, args.max_final_updates, q_idx, exact, args.precision)
+        run_e2e_step(X_pin, n, d, upd, emb, args.max_final_updates, q_idx, exact, args.precision, args.overlap)
         e2e_t, e2e_rec = [], []
         for _ in range(max(1, min(args.steps, 3))):
             flush_l2(flush)
-            dt, rec, _ = run_e2e_step(X_pin, n, d, upd, emb, args.max_final_updates, q_idx, exact, args.precision)
+            dt, rec, _ = run_e2e_step(X_pin, n, d, upd, emb, args.max_final_updates, q_idx, exact, args.precision,
+                                      args.overlap)
             e2e_t.append(dt)
             e2e_rec.append(rec)
         tmax = max_over_ranks(sum(e2e_t), world)

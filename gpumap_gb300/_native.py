@@ -32,7 +32,7 @@ class gm_params(C.Structure):
         ("negative_sample_rate", C.c_uint64), ("max_epoch", C.c_uint64), ("a", C.c_float),
         ("b", C.c_float), ("alpha", C.c_float), ("verbose", C.c_int32), ("metric", C.c_int32),
         ("n_instances", C.c_uint64), ("n_features", C.c_uint64), ("precision", C.c_int32),
-        ("device", C.c_int32),
+        ("device", C.c_int32), ("overlap", C.c_int32),
     ]
 
 

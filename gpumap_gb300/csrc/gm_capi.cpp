@@ -79,6 +79,7 @@ int gm_params_default(gm_params *out) {
   out->n_instances = 0;
   out->n_features = 0;
   out->precision = 0;
+  out->overlap = 0;
   out->device = -1;
   return GM_OK;
 }
@@ -121,6 +122,10 @@ int gm_run(gm_session *s, uint32_t ni, uint32_t nu, uint32_t ne, gm_result *out)
 
 int gm_get_embedding(const gm_session *s, gm_view *out) {
   if (!s || !out) return fail(GM_ERR_INVALID, "null argument");
+  // an overlapped embedding may still be running: the view is complete
+  // once it has finished
+  const int rc = guarded([&] { s->impl->drain(); });
+  if (rc != GM_OK) return rc;
   const auto &st = s->impl->state();
   out->ptr = st.emb;
   out->rows = s->impl->params().n_instances;
@@ -217,6 +222,8 @@ int gm_debug_copy(const gm_session *s, int which, void *host, uint64_t bytes) {
   int rc = gm_debug_buffer_size(s, which, &cap);
   if (rc) return rc;
   if (bytes > cap) return fail(GM_ERR_INVALID, "copy larger than buffer");
+  rc = guarded([&] { s->impl->drain(); });
+  if (rc != GM_OK) return rc;
   const auto &st = s->impl->state();
   const auto &es = s->impl->embed_scratch();
   const void *src = nullptr;

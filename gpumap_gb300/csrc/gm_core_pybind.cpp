@@ -150,6 +150,7 @@ PYBIND11_MODULE(_core, m) {
       GM_RW("n_instances", n_instances)
       GM_RW("n_features", n_features)
       GM_RW("precision", precision)
+      GM_RW("overlap", overlap)
       GM_RW("device", device);
 #undef GM_RW
 

@@ -52,6 +52,7 @@ Session::Session(const gm_params &p) : p_(p) {
     throw Error(GM_ERR_INVALID, "unknown metric");
   if (p.precision != 0 && p.precision != 1)
     throw Error(GM_ERR_INVALID, "precision must be 0 (FP32 NN-Descent) or 1 (exact, BF16 tensor cores)");
+  if (p.overlap != 0 && p.overlap != 1) throw Error(GM_ERR_INVALID, "overlap must be 0 or 1");
   if (p.n_instances > (uint64_t)(1u << 30))
     throw Error(GM_ERR_INVALID, "n_instances exceeds 2^30");
   if (p.n_features > (uint64_t)(1u << 24)) throw Error(GM_ERR_INVALID, "n_features too large");
@@ -60,6 +61,16 @@ Session::Session(const gm_params &p) : p_(p) {
   ck(cudaGetDevice(&device_), "cudaGetDevice");
   ck(cudaFree(nullptr), "CUDA context");
   ck(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  ck(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device_), "attr");
+  if (p.overlap) {
+    // the embedding stream gets the higher priority: its cooperative SGD
+    // launch is placed as soon as SMs free up
+    int lo = 0, hi = 0;
+    ck(cudaDeviceGetStreamPriorityRange(&lo, &hi), "stream priorities");
+    ck(cudaStreamCreateWithPriority(&estream_, cudaStreamNonBlocking, hi), "cudaStreamCreate");
+    ck(cudaEventCreateWithFlags(&ev_pub_, cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaEventCreateWithFlags(&ev_emb_, cudaEventDisableTiming), "cudaEventCreate");
+  }
 
   const size_t N = p.n_instances, d = p.n_features, k = p.n_neighbors;
   st_.n_cap = (int)N;
@@ -121,10 +132,15 @@ Session::Session(const gm_params &p) : p_(p) {
     es_.cap_partial = (Nm * k + 255) / 256 + 512;
     es_.partial = (float *)dalloc(es_.cap_partial * 2 * sizeof(float));
     es_.ipartial = (int *)dalloc(es_.cap_partial * sizeof(int));
-    es_.batch = d_batch_;
-    es_.tmp = d_tmp_;
+    // the embedding phase has its own batch, scan scratch, counters and
+    // pinned staging, so that it can run beside the other phases
+    es_.batch = (int *)dalloc(Nm * sizeof(int));
+    es_.tmp = (int *)dalloc(std::max(scan_tmp_ints((int)Nm), compact_tmp_ints((int)Nm)) *
+                            sizeof(int) + 64);
+    es_cnt_ = (int *)dalloc(16 * sizeof(int));
 
     ck(cudaMallocHost((void **)&h_pin_, (Nm + 64) * sizeof(uint32_t)), "cudaMallocHost");
+    ck(cudaMallocHost((void **)&h_emb_pin_, (Nm + 64) * sizeof(uint32_t)), "cudaMallocHost");
     if (p.precision == 1) {
       // split-BF16 shadow rows (hi | lo, 2 x dh bf16 each) plus a block of
       // distance / candidate scratch sized so that a block holds at most
@@ -151,7 +167,8 @@ Session::Session(const gm_params &p) : p_(p) {
     for (void *q : allocs_) cudaFree(q);
     allocs_.clear();
     if (h_pin_) cudaFreeHost(h_pin_);
-    if (stream_) cudaStreamDestroy(stream_);
+    if (h_emb_pin_) cudaFreeHost(h_emb_pin_);
+    release_streams();
     throw;
   }
 
@@ -186,18 +203,28 @@ Session::Session(const gm_params &p) : p_(p) {
       allocs_.clear();
       cudaFreeHost(h_pin_);
       h_pin_ = nullptr;
-      cudaStreamDestroy(stream_);
-      stream_ = nullptr;
+      cudaFreeHost(h_emb_pin_);
+      h_emb_pin_ = nullptr;
+      release_streams();
       throw Error(GM_ERR_CUDA, "cuTensorMapEncodeTiled unavailable or failed");
     }
-    ck(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, device_), "attr");
   }
   upd_q_.reset(N);
   ensure_embed(1);
 }
 
+void Session::release_streams() {
+  if (ev_pub_) cudaEventDestroy(ev_pub_);
+  if (ev_emb_) cudaEventDestroy(ev_emb_);
+  if (estream_) cudaStreamDestroy(estream_);
+  if (stream_) cudaStreamDestroy(stream_);
+  ev_pub_ = ev_emb_ = nullptr;
+  estream_ = stream_ = nullptr;
+}
+
 Session::~Session() {
   if (stream_) cudaStreamSynchronize(stream_);
+  if (estream_) cudaStreamSynchronize(estream_);
   for (auto &e : ev_pool_) cudaEventDestroy(e);
   for (auto &pr : ev_pending_) {
     cudaEventDestroy(pr.a);
@@ -220,10 +247,20 @@ Session::~Session() {
     cudaFree(es_.tmp2);
   }
   if (h_pin_) cudaFreeHost(h_pin_);
-  if (stream_) cudaStreamDestroy(stream_);
+  if (h_emb_pin_) cudaFreeHost(h_emb_pin_);
+  release_streams();
 }
 
 void Session::sync() { ck(cudaStreamSynchronize(stream_), "cudaStreamSynchronize"); }
+
+// Waits for every phase in flight, the overlapped embedding included, and
+// reports a device error bit raised meanwhile.
+void Session::drain() {
+  sync();
+  if (estream_) ck(cudaStreamSynchronize(estream_), "cudaStreamSynchronize");
+  emb_pending_ = false;
+  check_device_error("embedding");
+}
 
 void Session::check_device_error(const char *phase) {
   unsigned e = 0;
@@ -257,6 +294,7 @@ void Session::ensure_embed(size_t nb) {
   const size_t need = 2 * std::max<size_t>(nb, 1) * (size_t)st_.k;
   if (need <= es_.cap_coo) return;
   sync();
+  if (estream_) ck(cudaStreamSynchronize(estream_), "cudaStreamSynchronize");
   if (es_.coo_row) {
     cudaFree(es_.coo_row);
     cudaFree(es_.coo_col);
@@ -287,8 +325,9 @@ void Session::ensure_embed(size_t nb) {
 // ---------------------------------------------------------------------------
 // statistics: CUDA events around the launches of interest
 // ---------------------------------------------------------------------------
-void Session::timed_begin(int slot) {
+void Session::timed_begin(int slot, cudaStream_t s) {
   if (!stats_on_) return;
+  if (!s) s = stream_;
   cudaEvent_t a, b;
   if (ev_pool_.size() >= 2) {
     a = ev_pool_.back();
@@ -299,19 +338,27 @@ void Session::timed_begin(int slot) {
     cudaEventCreate(&a);
     cudaEventCreate(&b);
   }
-  cudaEventRecord(a, stream_);
+  cudaEventRecord(a, s);
   ev_pending_.push_back({a, b, slot});
 }
 
-void Session::timed_end(int slot) {
+void Session::timed_end(int slot, cudaStream_t s) {
   if (!stats_on_ || ev_pending_.empty()) return;
   (void)slot;
-  cudaEventRecord(ev_pending_.back().b, stream_);
+  cudaEventRecord(ev_pending_.back().b, s ? s : stream_);
 }
 
-void Session::collect_timings() {
+// Accumulates the event pairs in order; without `block`, stops at the first
+// pair still in flight (an overlapped embedding) and keeps the rest.
+void Session::collect_timings(bool block) {
   if (ev_pending_.empty()) return;
+  size_t done = 0;
   for (auto &pr : ev_pending_) {
+    if (!block && cudaEventQuery(pr.b) != cudaSuccess) {
+      cudaGetLastError();
+      break;
+    }
+    ++done;
     float ms = 0.0f;
     if (cudaEventSynchronize(pr.b) == cudaSuccess && cudaEventElapsedTime(&ms, pr.a, pr.b) == cudaSuccess) {
       if (pr.slot == 0) {
@@ -333,7 +380,7 @@ void Session::collect_timings() {
     ev_pool_.push_back(pr.a);
     ev_pool_.push_back(pr.b);
   }
-  ev_pending_.clear();
+  ev_pending_.erase(ev_pending_.begin(), ev_pending_.begin() + (long)done);
 }
 
 void Session::reset_stats() {
@@ -347,7 +394,8 @@ void Session::reset_stats() {
 
 void Session::get_stats(gm_stats *out) {
   sync();
-  collect_timings();
+  if (estream_) ck(cudaStreamSynchronize(estream_), "cudaStreamSynchronize");
+  collect_timings(true);
   unsigned long long h[16];
   ck(cudaMemcpy(h, d_stat_, sizeof(h), cudaMemcpyDeviceToHost), "stats");
   stats_.join_nodes = h[0];
@@ -416,13 +464,15 @@ gm_result Session::run(uint32_t n_ins, uint32_t n_upd, uint32_t n_emb) {
   if (n_emb != 0 && n_inserted_ != 0 && !emb_done_) {
     const auto t0 = Clock::now();
     r.n_embedding_ops = embed(n_emb);
-    sync();
-    check_device_error("embedding");
+    if (!p_.overlap) {
+      sync();
+      check_device_error("embedding");
+    }
     const auto t1 = Clock::now();
     r.embedding_time = std::chrono::duration<float>(t1 - t0).count();
     log("[GPUMAP] embed done: actual=%u time=%.3fs\n", r.n_embedding_ops, r.embedding_time);
   }
-  collect_timings();
+  collect_timings(!p_.overlap);
   stats_.phase_s[0] += r.insertion_time;
   stats_.phase_s[1] += r.update_time;
   stats_.phase_s[2] += r.embedding_time;
@@ -493,10 +543,14 @@ uint32_t Session::insert(uint32_t n_ops) {
   }
   // existing rows whose list changed, ascending
   compact_flags(st_.dirty, row0, -1, d_rows_, d_cnt_, d_tmp_, s);
+  // the embedding still in flight reads the published table and writes the
+  // embedding that embed_init reads: publish only after it
+  if (emb_pending_) ck(cudaStreamWaitEvent(s, ev_emb_, 0), "wait embedding");
   launch_adopt_and_publish(st_, row0, nb, d_rows_, d_cnt_, row0, n, s);
   launch_embed_init(st_, row0, nb, n, s);
   ck(cudaMemcpyAsync(h_pin_, d_cnt_, sizeof(int), cudaMemcpyDeviceToHost, s), "count");
   sync();
+  emb_pending_ = false;  // the stream waited for it above
   const int nd = (int)h_pin_[0];
   if (nd > 0) {
     ck(cudaMemcpyAsync(h_pin_, d_rows_, (size_t)nd * sizeof(int), cudaMemcpyDeviceToHost, s),
@@ -516,6 +570,8 @@ uint32_t Session::update(uint32_t n_ops, size_t &changed) {
   changed = 0;
   const size_t n = n_inserted_;
   if (n_ops == 0 || upd_done_ || n == 0) return 0;
+  // the update republishes rows the embedding in flight reads
+  if (emb_pending_) ck(cudaStreamWaitEvent(stream_, ev_emb_, 0), "wait embedding");
   const size_t threshold = (size_t)(0.0001f * (float)n);
   uint32_t left = n_ops;
   while (left > 0) {
@@ -629,28 +685,41 @@ uint32_t Session::embed(uint32_t n_ops) {
   const int nb = (int)batch.size();
   const int ni = (int)n;
   const int k = st_.k;
+  // overlap: the phase runs on its own stream once the table it reads is
+  // published; a previous embedding still in flight finishes first (its
+  // staging buffer and scratch are reused)
+  if (emb_pending_) ck(cudaEventSynchronize(ev_emb_), "wait embedding");
   cudaStream_t s = stream_;
+  if (p_.overlap) {
+    ck(cudaEventRecord(ev_pub_, stream_), "record publish");
+    ck(cudaStreamWaitEvent(estream_, ev_pub_, 0), "wait publish");
+    s = estream_;
+  }
   ensure_embed((size_t)nb);
-  std::memcpy(h_pin_, batch.data(), (size_t)nb * sizeof(uint32_t));
-  ck(cudaMemcpyAsync(d_batch_, h_pin_, (size_t)nb * sizeof(int), cudaMemcpyHostToDevice, s),
+  std::memcpy(h_emb_pin_, batch.data(), (size_t)nb * sizeof(uint32_t));
+  ck(cudaMemcpyAsync(es_.batch, h_emb_pin_, (size_t)nb * sizeof(int), cudaMemcpyHostToDevice, s),
      "batch");
   const int euclid = p_.metric == GM_METRIC_EUCLIDEAN;
   const double target = std::log2((double)(k - 1));
-  launch_fuzzy_graph(st_.pub_idx, st_.pub_dist, ni, k, euclid, d_batch_, nb, target, es_, s);
+  launch_fuzzy_graph(st_.pub_idx, st_.pub_dist, ni, k, euclid, es_.batch, nb, target, es_, s);
   if (sweeps_ > 2) emb_done_ = upd_done_;
   const uint64_t noise_seed = 42ull ^ (uint64_t)sweeps_;
-  launch_add_noise(st_.emb, ni, d_batch_, nb, 0.001f, noise_seed, es_, s);
+  launch_add_noise(st_.emb, ni, es_.batch, nb, 0.001f, noise_seed, es_, s);
   launch_schedule(ni, nb, k, p_.alpha, (int)p_.max_epoch, (int)p_.negative_sample_rate, es_, s);
   launch_set_int(es_.iscal + kIscalN, ni, s);
-  timed_begin(2);
-  run_sgd();
-  timed_end(2);
+  timed_begin(2, s);
+  run_sgd(s);
+  timed_end(2, s);
   const int nu = ni - nb;
   if (nu > 0) {
     ck(cudaMemsetAsync(es_.flag, 0, (size_t)ni * sizeof(int), s), "flags");
-    launch_mark_rows(d_batch_, nb, es_.flag, s);
-    compact_flags(es_.flag, ni, 0, es_.unsel, d_cnt_ + 4, d_tmp_, s);
+    launch_mark_rows(es_.batch, nb, es_.flag, s);
+    compact_flags(es_.flag, ni, 0, es_.unsel, es_cnt_, es_.tmp, s);
     launch_heuristic(st_.pub_idx, st_.pub_dist, ni, k, euclid, es_.unsel, nu, st_.emb, es_, s);
+  }
+  if (p_.overlap) {
+    ck(cudaEventRecord(ev_emb_, s), "record embedding");
+    emb_pending_ = true;
   }
   return (uint32_t)nb;
 }
@@ -659,19 +728,24 @@ uint32_t Session::embed(uint32_t n_ops) {
 // with a grid barrier between epochs (sizes are read from device scalars).
 // t_col (free once the schedule is built) holds the edge grouping and
 // ipartial its bins.
-void Session::run_sgd() {
+void Session::run_sgd(cudaStream_t s) {
   if (p_.max_epoch == 0) return;
+  // overlapped: half the SMs, the other half stays free for the next
+  // cycle's distance work (the per-epoch time does not depend on it)
+  const int max_ctas = p_.overlap ? std::max(1, sms_ / 2) : 0;
   ck(launch_sgd_persistent(st_.emb, es_.t_row, es_.flag_tail, es_.t_val, es_.next_s, es_.next_n,
                            es_.iscal, es_.fscal, p_.alpha, 1.0f, p_.a, p_.b, (int)p_.max_epoch,
                            (int)p_.negative_sample_rate, 42ull, es_.t_col, es_.ipartial,
-                           (unsigned *)(es_.iscal + kIscalBarrier), st_.err, device_, stream_,
-                           st_.stat),
+                           (unsigned *)(es_.iscal + kIscalBarrier), st_.err, device_, s, st_.stat,
+                           max_ctas),
      "SGD launch");
 }
 
 void Session::close() {
   if (closed_) return;
   cudaStreamSynchronize(stream_);
+  if (estream_) cudaStreamSynchronize(estream_);
+  emb_pending_ = false;
   closed_ = true;
 }
 
@@ -679,6 +753,7 @@ void Session::debug_scalars(int64_t *out, int cnt) const {
   int iscal[16] = {0};
   unsigned err = 0;
   cudaStreamSynchronize(stream_);
+  if (estream_) cudaStreamSynchronize(estream_);
   cudaMemcpy(iscal, es_.iscal, sizeof(iscal), cudaMemcpyDeviceToHost);
   cudaMemcpy(&err, st_.err, sizeof(err), cudaMemcpyDeviceToHost);
   int64_t v[11] = {(int64_t)n_inserted_,

@@ -71,6 +71,7 @@ class Session {
   cudaStream_t stream() const { return stream_; }
   int device() const { return device_; }
   void set_stats(bool on) { stats_on_ = on; }
+  void drain();
   void get_stats(gm_stats *out);
   void reset_stats();
   void debug_scalars(int64_t *out, int n) const;
@@ -90,14 +91,20 @@ class Session {
   void ensure_embed(size_t nb);
   template <typename... A> void log(const char *fmt, A... a) const;
   void sync();
-  void timed_begin(int slot);
-  void timed_end(int slot);
-  void collect_timings();
-  void run_sgd();
+  void release_streams();
+  void timed_begin(int slot, cudaStream_t s = nullptr);
+  void timed_end(int slot, cudaStream_t s = nullptr);
+  void collect_timings(bool block = true);
+  void run_sgd(cudaStream_t s);
 
   gm_params p_;
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
+  // overlap mode: the embedding phase's stream, "table published" and
+  // "embedding done" events, and whether an embedding is in flight
+  cudaStream_t estream_ = nullptr;
+  cudaEvent_t ev_pub_ = nullptr, ev_emb_ = nullptr;
+  bool emb_pending_ = false;
   DevState st_;
   UpdScratch us_;
   EmbedScratch es_;
@@ -112,7 +119,9 @@ class Session {
   int *d_rows_ = nullptr, *d_rows2_ = nullptr, *d_batch_ = nullptr;
   int *d_cnt_ = nullptr;  // [0] list count, [1] edges, [2] report count, [3] join count
   int *d_tmp_ = nullptr;
-  uint32_t *h_pin_ = nullptr;  // pinned staging (n_cap + 16 words)
+  uint32_t *h_pin_ = nullptr;      // pinned staging (n_cap + 16 words)
+  uint32_t *h_emb_pin_ = nullptr;  // the embedding phase's pinned staging
+  int *es_cnt_ = nullptr;          // the embedding phase's compaction counter
 
   size_t n_inserted_ = 0;
   size_t ins_head_ = 0;      // insertion queue = [ins_head_, n_inserted_)

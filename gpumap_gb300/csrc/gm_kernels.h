@@ -195,7 +195,8 @@ void launch_sgd(float *emb, const int *head, const int *tail, const float *eps,
                 int neg_rate, uint64_t seed, cudaStream_t s,
                 unsigned long long *stat = nullptr);
 // All n_epochs epochs in one cooperative launch (one CTA of 512 threads per
-// SM) with a bounded grid barrier between epochs; bar: 1 device word,
+// SM, at most max_ctas CTAs when max_ctas > 0) with a bounded grid barrier
+// between epochs; bar: 1 device word,
 // cleared here; a barrier timeout sets kDevErrSpin in *err.  perm (nnz ints)
 // and bins (kSgdEpsBins ints), when given, receive the edges grouped by
 // sampling period (threads of a warp then tend to be active together).
@@ -206,7 +207,7 @@ cudaError_t launch_sgd_persistent(float *emb, const int *head, const int *tail,
                                   float gamma, float a, float b, int n_epochs, int neg_rate,
                                   uint64_t seed, int *perm, int *bins, unsigned *bar,
                                   unsigned *err, int device, cudaStream_t s,
-                                  unsigned long long *stat = nullptr);
+                                  unsigned long long *stat = nullptr, int max_ctas = 0);
 void launch_set_int(int *p, int v, cudaStream_t s);
 constexpr int kIscalN = 4;
 constexpr int kIscalBarrier = 8;  // iscal[8..9]: SGD grid-barrier words

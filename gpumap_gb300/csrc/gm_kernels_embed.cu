@@ -889,9 +889,10 @@ cudaError_t launch_sgd_persistent(float *emb, const int *head, const int *tail,
                                   float gamma, float a, float b, int n_epochs, int neg_rate,
                                   uint64_t seed, int *perm, int *bins, unsigned *bar,
                                   unsigned *err, int device, cudaStream_t s,
-                                  unsigned long long *stat) {
+                                  unsigned long long *stat, int max_ctas) {
   if (n_epochs <= 0) return cudaSuccess;
-  const int grid = sgd_persistent_grid(device);
+  int grid = sgd_persistent_grid(device);
+  if (max_ctas > 0) grid = std::min(grid, max_ctas);
   if (grid <= 0) return cudaErrorInvalidDevice;
   cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;

@@ -55,6 +55,11 @@ typedef struct gm_params {
                                     1 = exact insertion: BF16 tensor-core distance tiles against
                                         every inserted row, FP32 re-score of the survivors */
   int32_t device;                /* CUDA device ordinal, -1 = current */
+  int32_t overlap;               /* 0 = phases run one after another, as the reference (default);
+                                    1 = a cycle's embedding runs on a second stream while the next
+                                        cycle's distance work proceeds: gm_run returns once the
+                                        embedding is queued (embedding_time is then the time to
+                                        queue it), gm_get_embedding waits for it */
 } gm_params;
 
 /* Result of one cycle (reference GPUMAPResult, gpumap.cuh:38-56). */

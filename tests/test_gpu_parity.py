@@ -244,3 +244,40 @@ def test_exact_mode_bitexact(native, oracle_mod, d, metric, k):
     ei, _ = exact_knn(X, k, metric="cosine" if metric else "euclidean")
     idx = s.copy("pub_idx", U32).reshape(n, k + 1)[:, :k]
     assert recall_at_k(idx, ei) > 0.99
+
+
+# ---------------------------------------------------------------------------
+# overlap = 1: each cycle's embedding runs on its own stream beside the next
+# cycle's distance work; everything the oracle pins must be unchanged
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("precision,upd", [(1, 0), (1, 300), (0, 300)])
+def test_overlap_mode_bitexact(native, oracle_mod, precision, upd):
+    n, d, k = 2400, 40, 15
+    X, _ = gaussian_mixture(n, d, seed=77)
+    s = native.Session(native.default_params(n_instances=n, n_features=d, n_neighbors=k, max_epoch=30,
+                                             device=0, precision=precision, overlap=1))
+    o = oracle_mod.OracleSession(n, d, k=k, max_epoch=30, precision=precision)
+    step = 400
+    for c in range(n // step):
+        chunk = X[c * step : (c + 1) * step]
+        s.append_host(chunk)
+        o.append(chunk)
+        same_result(s.run(step, upd, 500), o.run(step, upd, 500))
+        # two cycles back to back, then the state (the copies wait for the
+        # embedding in flight)
+        if c % 2 == 1:
+            same_state(s, o, embed=True, tag=f"overlap cycle {c}")
+    emb = s.copy("embedding", F32).reshape(n, 2)
+    assert np.all(np.isfinite(emb))
+    # the SGD is Hogwild-parallel: compare its outcome with the same build
+    # without overlap statistically
+    r = native.Session(native.default_params(n_instances=n, n_features=d, n_neighbors=k, max_epoch=30,
+                                             device=0, precision=precision, overlap=0))
+    for c in range(n // step):
+        r.append_host(X[c * step : (c + 1) * step])
+        r.run(step, upd, 500)
+    ref = r.copy("embedding", F32).reshape(n, 2)
+    t_ov, t_ref = trustworthiness(X, emb, n_neighbors=k), trustworthiness(X, ref, n_neighbors=k)
+    assert abs(t_ov - t_ref) < 0.02, (t_ov, t_ref)
+    s.close()
+    r.close()

@@ -281,3 +281,19 @@ def test_overlap_mode_bitexact(native, oracle_mod, precision, upd):
     assert abs(t_ov - t_ref) < 0.02, (t_ov, t_ref)
     s.close()
     r.close()
+
+
+@pytest.mark.parametrize("n,d,metric,k,step", [(8, 3, 0, 15, 3), (40, 5, 1, 10, 7), (300, 17, 0, 32, 64)])
+def test_exact_mode_small_and_ragged(native, oracle_mod, n, d, metric, k, step):
+    # fewer rows than list slots, batches that are not multiples of anything,
+    # odd feature counts (shadow rows padded to 64), the largest k
+    X, _ = gaussian_mixture(n, d, seed=n + d)
+    s = native.Session(native.default_params(n_instances=n, n_features=d, n_neighbors=k, metric=metric,
+                                             max_epoch=10, device=0, precision=1))
+    o = oracle_mod.OracleSession(n, d, k=k, metric=metric, max_epoch=10, precision=1)
+    for c0 in range(0, n, step):
+        chunk = X[c0 : c0 + step]
+        s.append_host(chunk)
+        o.append(chunk)
+        same_result(s.run(len(chunk), 50, 50), o.run(len(chunk), 50, 50))
+        same_state(s, o, embed=True, tag=f"rows {c0}+{len(chunk)}")

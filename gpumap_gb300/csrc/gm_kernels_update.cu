@@ -173,7 +173,7 @@ struct LJSmem {
   int nN, nC;
 };
 
-__global__ void __launch_bounds__(kLJThreads) k_local_join(
+__global__ void __launch_bounds__(kLJThreads, 3) k_local_join(
     const int *join_nodes, const int *n_join_dev, const int *fwd_new,
     const int *fwd_old, const int *rev_new, const int *rev_old, const int4 *sizes,
     const float *X, const float *norms, int ld, int d, int n, int k, Key *g_key,
@@ -186,44 +186,49 @@ __global__ void __launch_bounds__(kLJThreads) k_local_join(
   for (int bi = blockIdx.x; bi < n_join; bi += gridDim.x) {
     __syncthreads();  // previous node's shared data is no longer read
     const int u = join_nodes[bi];
-    if (t == 0) {
+    if (warp == 0) {
+      // join lists built by warp 0, entries in sample order (ballot
+      // compaction): N = forward-new ++ reverse-new not already in
+      // forward-new, then forward-old ++ reverse-old not in forward-old
       const int4 sz = sizes[u];
-      int nN = 0;
+      const unsigned lt = (1u << lane) - 1u;
       const int *fn = fwd_new + (size_t)u * kSamples;
       const int *rn = rev_new + (size_t)u * kSamples;
       const int *fo = fwd_old + (size_t)u * kSamples;
       const int *ro = rev_old + (size_t)u * kSamples;
-      for (int s = 0; s < sz.x; ++s) {
-        const int v = fn[s];
-        if (v >= 0 && v < n) S.cid[nN++] = v;
-      }
-      const int nfn = nN;
-      for (int s = 0; s < sz.y; ++s) {
-        const int v = rn[s];
-        if (v < 0 || v >= n) continue;
-        bool seen = false;
-        for (int q = 0; q < nfn; ++q) seen |= (S.cid[q] == v);
-        if (!seen) S.cid[nN++] = v;
-      }
-      int nC = nN;
-      for (int s = 0; s < sz.z; ++s) {
-        const int v = fo[s];
-        if (v >= 0 && v < n) S.cid[nC++] = v;
-      }
-      const int nfo = nC;
-      for (int s = 0; s < sz.w; ++s) {
-        const int v = ro[s];
-        if (v < 0 || v >= n) continue;
-        bool seen = false;
-        for (int q = nN; q < nfo; ++q) seen |= (S.cid[q] == v);
-        if (!seen) S.cid[nC++] = v;
-      }
-      S.nN = nN;
-      S.nC = nC;
-      if (stat && nN > 0) {
-        atomicAdd(&stat[0], 1ull);
-        atomicAdd(&stat[1], (unsigned long long)nC);
-        atomicAdd(&stat[2], (unsigned long long)nN * (unsigned long long)nC);
+      int v = lane < sz.x ? fn[lane] : -1;
+      bool ok = v >= 0 && v < n;
+      unsigned bal = __ballot_sync(0xffffffffu, ok);
+      if (ok) S.cid[__popc(bal & lt)] = v;
+      const int nfn = __popc(bal);
+      __syncwarp();
+      v = lane < sz.y ? rn[lane] : -1;
+      ok = v >= 0 && v < n;
+      for (int q = 0; q < nfn && ok; ++q) ok = S.cid[q] != v;
+      bal = __ballot_sync(0xffffffffu, ok);
+      if (ok) S.cid[nfn + __popc(bal & lt)] = v;
+      const int nN = nfn + __popc(bal);
+      __syncwarp();
+      v = lane < sz.z ? fo[lane] : -1;
+      ok = v >= 0 && v < n;
+      bal = __ballot_sync(0xffffffffu, ok);
+      if (ok) S.cid[nN + __popc(bal & lt)] = v;
+      const int nfo = nN + __popc(bal);
+      __syncwarp();
+      v = lane < sz.w ? ro[lane] : -1;
+      ok = v >= 0 && v < n;
+      for (int q = nN; q < nfo && ok; ++q) ok = S.cid[q] != v;
+      bal = __ballot_sync(0xffffffffu, ok);
+      if (ok) S.cid[nfo + __popc(bal & lt)] = v;
+      const int nC = nfo + __popc(bal);
+      if (lane == 0) {
+        S.nN = nN;
+        S.nC = nC;
+        if (stat && nN > 0) {
+          atomicAdd(&stat[0], 1ull);
+          atomicAdd(&stat[1], (unsigned long long)nC);
+          atomicAdd(&stat[2], (unsigned long long)nN * (unsigned long long)nC);
+        }
       }
     }
     __syncthreads();
@@ -241,30 +246,47 @@ __global__ void __launch_bounds__(kLJThreads) k_local_join(
 #pragma unroll
       for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
 
-    for (int k0 = 0; k0 < d; k0 += kLJKC) {
+    // feature chunks: the next chunk's loads are issued before this chunk's
+    // products, so their latency overlaps the arithmetic
+    float4 pa[2], pb[4];
+    auto fetch = [&](int k0) {
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
         const int f = t + p * kLJThreads;
         const int r = f >> 3, q = f & 7;
         const int col = k0 + 4 * q;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        pa[p] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (r < nN && col < ld)
-          v = __ldg(reinterpret_cast<const float4 *>(X + (size_t)S.cid[r] * ld + col));
-        S.As[4 * q][r] = v.x; S.As[4 * q + 1][r] = v.y;
-        S.As[4 * q + 2][r] = v.z; S.As[4 * q + 3][r] = v.w;
+          pa[p] = __ldg(reinterpret_cast<const float4 *>(X + (size_t)S.cid[r] * ld + col));
       }
 #pragma unroll
       for (int p = 0; p < 4; ++p) {
         const int f = t + p * kLJThreads;
         const int r = f >> 3, q = f & 7;
         const int col = k0 + 4 * q;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        pb[p] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (r < nC && col < ld)
-          v = __ldg(reinterpret_cast<const float4 *>(X + (size_t)S.cid[r] * ld + col));
-        S.Bs[4 * q][r] = v.x; S.Bs[4 * q + 1][r] = v.y;
-        S.Bs[4 * q + 2][r] = v.z; S.Bs[4 * q + 3][r] = v.w;
+          pb[p] = __ldg(reinterpret_cast<const float4 *>(X + (size_t)S.cid[r] * ld + col));
+      }
+    };
+    fetch(0);
+    for (int k0 = 0; k0 < d; k0 += kLJKC) {
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        const int f = t + p * kLJThreads;
+        const int r = f >> 3, q = f & 7;
+        S.As[4 * q][r] = pa[p].x; S.As[4 * q + 1][r] = pa[p].y;
+        S.As[4 * q + 2][r] = pa[p].z; S.As[4 * q + 3][r] = pa[p].w;
+      }
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        const int f = t + p * kLJThreads;
+        const int r = f >> 3, q = f & 7;
+        S.Bs[4 * q][r] = pb[p].x; S.Bs[4 * q + 1][r] = pb[p].y;
+        S.Bs[4 * q + 2][r] = pb[p].z; S.Bs[4 * q + 3][r] = pb[p].w;
       }
       __syncthreads();
+      if (k0 + kLJKC < d) fetch(k0 + kLJKC);
       if (active) {
         const int kend = min(kLJKC, d - k0);
         for (int kk = 0; kk < kend; ++kk) {

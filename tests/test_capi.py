@@ -59,7 +59,8 @@ def test_pybind_surface(native):
 
 def test_invalid_params_rejected_before_device(native):
     # parameter validation happens before any CUDA call
-    for kw in ({"n_components": 3}, {"n_neighbors": 33}, {"n_neighbors": 0}, {"metric": 7}, {"precision": 2}):
+    for kw in ({"n_components": 3}, {"n_neighbors": 33}, {"n_neighbors": 0}, {"metric": 7}, {"precision": 2},
+               {"overlap": 2}):
         p = native.default_params(n_instances=10, n_features=4, **kw)
         with pytest.raises(ValueError):
             native.Session(p)

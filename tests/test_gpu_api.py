@@ -92,3 +92,23 @@ def test_append_validation_errors():
         gm.GPUMAP(ArrayDataLoader(np.zeros((3, 4), np.float32)), p2)
     cai = core.get_neighbor_indices().__cuda_array_interface__
     assert cai["shape"] == (10, 16) and cai["typestr"] == "<u4" and cai["data"][1] is True
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_overlap_through_python_api(precision):
+    # overlap = 1 from Python: the k-NN tables equal the non-overlapped
+    # build's, get_embedding waits for the embedding still in flight
+    import torch
+
+    X, a = _model(n=2000, d=24, seed=5, precision=precision, overlap=1)
+    _, b = _model(n=2000, d=24, seed=5, precision=precision, overlap=0)
+    assert a.params.overlap == 1
+    for _ in range(4):
+        a.run_with_n_ops(500, 300, 600)
+        b.run_with_n_ops(500, 300, 600)
+    emb = a.get_embedding()
+    assert tuple(emb.shape) == (2000, 2) and torch.isfinite(emb).all()
+    assert torch.equal(a.get_neighbor_indices(), b.get_neighbor_indices())
+    assert torch.equal(a.get_neighbor_dists(), b.get_neighbor_dists())
+    a.close()
+    b.close()

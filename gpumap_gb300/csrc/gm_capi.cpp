@@ -355,6 +355,7 @@ int gm_op_sgd(float *emb, int64_t n, const int32_t *head, const int32_t *tail,
               float a, float b, int32_t n_epochs, int32_t neg_rate, uint64_t seed,
               void *stream) {
   if (n < 1 || nnz < 0 || n_epochs < 0) return fail(GM_ERR_INVALID, "bad sizes");
+  if ((uintptr_t)emb % 8 != 0) return fail(GM_ERR_INVALID, "emb must be 8-byte aligned");
   cudaStream_t s = (cudaStream_t)stream;
   return guarded([&] {
     if (nnz == 0 || n_epochs == 0) return;

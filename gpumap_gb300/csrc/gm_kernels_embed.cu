@@ -442,8 +442,9 @@ GM_D void sgd_edge(float *emb, int row, int j, int kk, float ep, float &ns, floa
   cur0 = __fadd_rn(cur0, g0);
   cur1 = __fadd_rn(cur1, g1);
   const float t0 = trunc_grad(rounding, -g0), t1 = trunc_grad(rounding, -g1);
-  atomicAdd(op, t0);
-  atomicAdd(op + 1, t1);
+  // both coordinates in one vector reduction (each element added
+  // atomically, exactly as two scalar adds; rows are 8-byte aligned)
+  atomicAdd(reinterpret_cast<float2 *>(op), make_float2(t0, t1));
   ns = __fadd_rn(ns, ep);
   if (n_neg > 0) {
     const float two_gb = __fmul_rn(__fmul_rn(2.0f, gamma), b);
@@ -489,8 +490,8 @@ GM_D void sgd_edge(float *emb, int row, int j, int kk, float ep, float &ns, floa
     nn = __fadd_rn(nn, __fmul_rn((float)n_neg, ep_neg));
     my_negs += (unsigned)n_neg;
   }
-  atomicAdd(cp, trunc_grad(rounding, g0));
-  atomicAdd(cp + 1, trunc_grad(rounding, g1));
+  atomicAdd(reinterpret_cast<float2 *>(cp),
+            make_float2(trunc_grad(rounding, g0), trunc_grad(rounding, g1)));
 }
 
 // Edges [first, nnz) step stride of one epoch, state in global memory.

@@ -80,6 +80,7 @@ extern "C" int gm_op_sgd_noalloc(float *emb, int64_t n, const int32_t *head, con
                               "gm_op_sgd_noalloc: nnz exceeds its fixed scratch of 1048576 edges; "
                               "use gm_op_sgd for larger edge lists");
   if (n > INT32_MAX) return gm::set_last_error(GM_ERR_INVALID, "n exceeds int32 range");
+  if ((uintptr_t)emb % 8 != 0) return gm::set_last_error(GM_ERR_INVALID, "emb must be 8-byte aligned");
   float *base = nullptr;
   const int rc = scratch_address(&base);
   if (rc != GM_OK) return rc;

@@ -67,7 +67,8 @@ int gm_op_fuzzy_schedule(const uint32_t *pub_idx, const float *pub_dist, int64_t
                          float *scalars_out, void *stream);
 
 /* SGD epochs on a scheduled edge list (reference optimize_batch_kernel loop,
- * embedding_kernel.cuh:509-589 and :780-797). emb: n x 2 device, updated. */
+ * embedding_kernel.cuh:509-589 and :780-797). emb: n x 2 device, updated,
+ * 8-byte aligned (GM_ERR_INVALID otherwise). */
 int gm_op_sgd(float *emb, int64_t n, const int32_t *head, const int32_t *tail,
               const float *eps, int64_t nnz, float rounding, float alpha0, float gamma,
               float a, float b, int32_t n_epochs, int32_t negative_sample_rate,

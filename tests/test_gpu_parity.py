@@ -269,8 +269,11 @@ def test_overlap_mode_bitexact(native, oracle_mod, precision, upd):
             same_state(s, o, embed=True, tag=f"overlap cycle {c}")
     emb = s.copy("embedding", F32).reshape(n, 2)
     assert np.all(np.isfinite(emb))
-    # the SGD is Hogwild-parallel: compare its outcome with the same build
-    # without overlap statistically
+    # the SGD is Hogwild-parallel (and uses half the SMs here, so its update
+    # order differs): compare its outcome with the same build without
+    # overlap statistically.  Repeated runs of either mode at this size gave
+    # trustworthiness 0.81-0.85 with precision 0 (approximate lists) and
+    # 0.9588-0.9594 with precision 1 (exact lists).
     r = native.Session(native.default_params(n_instances=n, n_features=d, n_neighbors=k, max_epoch=30,
                                              device=0, precision=precision, overlap=0))
     for c in range(n // step):
@@ -278,7 +281,8 @@ def test_overlap_mode_bitexact(native, oracle_mod, precision, upd):
         r.run(step, upd, 500)
     ref = r.copy("embedding", F32).reshape(n, 2)
     t_ov, t_ref = trustworthiness(X, emb, n_neighbors=k), trustworthiness(X, ref, n_neighbors=k)
-    assert abs(t_ov - t_ref) < 0.02, (t_ov, t_ref)
+    tol = 0.05 if precision == 0 else 0.01
+    assert abs(t_ov - t_ref) < tol, (t_ov, t_ref)
     s.close()
     r.close()
 

@@ -6,8 +6,8 @@
 * ``oracle/_ref/queue_golden`` -- when the reference tree is present, the
   reference's own cpp/src/queue.cuh (plain C++, no RAFT/RMM) compiled in place
   with the driver ``oracle/ref_queue_driver.cpp``; used to regenerate the
-  committed queue fixtures.  The rest of the reference cannot be built here
-  (RAFT/RMM and CUDA 12.6 are required).
+  committed queue fixtures.  The reference's CUDA path is built separately by
+  oracle/refbuild/build_ref.py.
 """
 from __future__ import annotations
 
@@ -20,7 +20,8 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-REFERENCE = Path("/root/reference")
+# the reference tree: GPUMAP_REFERENCE, else the read-only mount this recipe was written against
+REFERENCE = Path(os.environ.get("GPUMAP_REFERENCE", "/root/reference"))
 
 
 def _run(cmd, verbose):

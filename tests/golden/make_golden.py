@@ -1,6 +1,7 @@
 """Regenerates the committed golden fixtures from the reference itself.
 
-Run in a container that has the reference tree at /root/reference:
+Run where the reference tree is available (its root in GPUMAP_REFERENCE,
+else the read-only mount this script was written against):
 
     python tests/golden/make_golden.py
 
@@ -25,7 +26,9 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
-REF_PY = Path("/root/reference/python")
+import os
+
+REF_PY = Path(os.environ.get("GPUMAP_REFERENCE", "/root/reference")) / "python"
 
 
 def import_reference():

@@ -103,3 +103,53 @@ def test_persistent_estimator_roundtrip(tmp_path):
     q = PersistentEstimator(MeanRateEstimator(), str(db), "update")
     assert q.estimate_ops(2.0) == ref
     q.close()
+
+
+# ---- the reference's own CUDA fuzzy set and edge schedule ------------------
+# Fixtures: tests/golden/ref_fuzzy_<case>.in (published k-NN tables from the
+# oracle's progressive cycles) and .out (what the reference's own
+# compute_fuzzy_graph, trim_graph, make_epochs_per_sample_kernel and
+# compute_rounding_factor produced from them on a GB300, through
+# oracle/refbuild/ref_fuzzy_driver.cu); tests/golden/make_ref_fuzzy.py makes both.
+REF_FUZZY_CASES = ["euclid_k15", "euclid_k15_partial", "cosine_k10", "euclid_k30", "tiny_sentinels"]
+
+
+def _sorted_by_edge(rows, cols, vals):
+    order = np.lexsort((cols, rows))
+    return rows[order], cols[order], vals[order]
+
+
+@pytest.mark.parametrize("case", REF_FUZZY_CASES)
+def test_fuzzy_schedule_matches_reference_build(oracle_mod, case):
+    import sys
+
+    sys.path.insert(0, str(GOLD))
+    from make_ref_fuzzy import read_input, read_output
+
+    c = read_input(GOLD / f"ref_fuzzy_{case}.in")
+    r = read_output(GOLD / f"ref_fuzzy_{case}.out", c["n"])
+    o = oracle_mod.fuzzy_schedule(c["pub_idx"], c["pub_dist"], c["k"], c["euclidean"], c["batch"],
+                                  c["n_epochs"], c["alpha"])
+    # integer work is bit-exact: the fuzzy-union COO and the trimmed schedule,
+    # compared as sorted (row, col) lists (the reference appends by atomics)
+    assert (o["nnz"], o["extras"], o["nnz2"]) == (r["nnz"], r["extras"], r["nnz2"])
+    rr, rc, rv = _sorted_by_edge(r["coo_row"], r["coo_col"], r["coo_val"])
+    orr, orc, ov = _sorted_by_edge(o["coo_row"], o["coo_col"], o["coo_val"])
+    np.testing.assert_array_equal(orr, rr)
+    np.testing.assert_array_equal(orc, rc)
+    tr, tc, te = _sorted_by_edge(r["t_row"], r["t_col"], r["t_eps"])
+    otr, otc, ote = _sorted_by_edge(o["t_row"], o["t_col"], o["t_eps"])
+    np.testing.assert_array_equal(otr, tr)
+    np.testing.assert_array_equal(otc, tc)
+    assert o["rounding"] == r["rounding"] and o["max_w"] == r["max_w"]
+    np.testing.assert_array_equal(o["rho"], r["rho"])
+    # floating point: the reference bisects sigma on an FP32 sum of __expf
+    # terms, the oracle on an FP64 sum of its own expf; the bisection may stop
+    # one step apart (|psum - target| < 1e-5), which moves sigma by < 1e-5
+    # relative and a weight exp(-(d - rho) / sigma) by up to a few e-5.
+    srel = np.abs(o["sigma"] - r["sigma"]) / np.maximum(np.abs(r["sigma"]), 1e-30)
+    assert srel.max() <= 1e-5, srel.max()
+    for mine, ref in ((ov, rv), (ote, te)):
+        rel = np.abs(mine - ref) / np.maximum(np.abs(ref), 1e-30)
+        assert np.mean(rel <= 1e-5) >= 0.999, np.mean(rel <= 1e-5)
+        assert rel.max() <= 3e-5, rel.max()

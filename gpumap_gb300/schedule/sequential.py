@@ -1,14 +1,18 @@
-"""Insertion, then update, then embedding: the whole budget goes to the first
-unfinished operation (reference: python/gpumap/schedule/sequential.py)."""
+"""One operation at a time (reference python/gpumap/schedule/sequential.py:9-52)."""
 from __future__ import annotations
 
 from typing import Optional
 
-from .estimator import Estimator, MeanRateEstimator
-from .strategy import BaseStrategy
+from .estimator import Estimator
+from .strategy import OPERATIONS, UINT32_MAX, BaseStrategy
 
 
 class SequentialPriorityStrategy(BaseStrategy):
+    """Insertion until it finishes, then update until it finishes, then
+    embedding: the first unfinished operation gets an unbounded op count (the
+    engine stops it when its work runs out) and the other two none.  The
+    estimators still learn from every cycle."""
+
     def __init__(
         self,
         n_instances: int,
@@ -20,24 +24,11 @@ class SequentialPriorityStrategy(BaseStrategy):
         confidence: float = 0.95,
         min_insertion_ops: int = 500,
     ):
-        super().__init__(
-            weights=(1.0, 1.0, 1.0),
-            reserved=0.1,
-            insertion_estimator=insertion_estimator or MeanRateEstimator(),
-            update_estimator=update_estimator or MeanRateEstimator(),
-            embedding_estimator=embedding_estimator or MeanRateEstimator(),
-            n_instances=n_instances,
-            n_neighbors=n_neighbors,
-            default_n_ops=default_n_ops,
-            confidence=confidence,
-            min_insertion_ops=min_insertion_ops,
-        )
-        self._update_counter = 0
+        super().__init__(weights=(1.0, 1.0, 1.0), reserved=0.1, insertion_estimator=insertion_estimator,
+                         update_estimator=update_estimator, embedding_estimator=embedding_estimator,
+                         n_instances=n_instances, n_neighbors=n_neighbors, default_n_ops=default_n_ops,
+                         confidence=confidence, min_insertion_ops=min_insertion_ops)
 
     def allocate(self, target_latency: float) -> tuple[int, int, int]:
-        for i in range(3):
-            if not self.completeness[i]:
-                out = [0, 0, 0]
-                out[i] = self.max_uint32
-                return tuple(out)
-        return (0, 0, self.max_uint32)
+        active = next((op for op in OPERATIONS if not self._done[op]), OPERATIONS[-1])
+        return tuple(UINT32_MAX if op == active else 0 for op in OPERATIONS)

@@ -16,7 +16,10 @@ of them is used here.  Instead:
   only) and the pybind11 headers bundled with PyTorch, into the extension
   ``baseline/_ref/gpumap/_core``, next to an unmodified copy of the
   reference's Python package.  That is the layout ``pip install --target
-  baseline/_ref`` would have produced.  It also compiles the test driver
+  baseline/_ref`` would have produced.  One object is added to the module:
+  ``zeroed_new.cpp``, a zero-filling operator new with hidden visibility,
+  which makes an uninitialised read in the reference's Bloom filter
+  deterministic (the file says why).  It also compiles the test driver
   ``oracle/refbuild/ref_fuzzy_driver.cu`` (the reference's own fuzzy-set and
   edge-scheduling functions on a k-NN table read from a file) into
   ``baseline/_ref/bin/ref_fuzzy_driver``.
@@ -111,7 +114,9 @@ def build(verbose: bool = False) -> Path | None:
     if not (cpp / "src" / "impl.cu").exists():
         return None
     out = core_path()
-    deps = sorted(cpp.rglob("*.cu*")) + sorted(SHIM.rglob("*.h*")) + [HERE / "ref_fuzzy_driver.cu"]
+    deps = sorted(cpp.rglob("*.cu*")) + sorted(SHIM.rglob("*.h*")) + [HERE / "ref_fuzzy_driver.cu",
+                                                                      HERE / "zeroed_new.cpp",
+                                                                      HERE / "zeroed_new.map"]
     OBJ.mkdir(parents=True, exist_ok=True)
     PKG_OUT.mkdir(parents=True, exist_ok=True)
     # the reference's Python package, unmodified
@@ -133,6 +138,10 @@ def build(verbose: bool = False) -> Path | None:
            f"-I{_torch_include()}", f"-I{sysconfig.get_paths()['include']}"]
     units = [cpp / "bindings" / "binding.cu", cpp / "src" / "impl.cu"]
     cmds = [[nvcc, *ARCH, *FLAGS, *inc, "-c", str(u), "-o", str(OBJ / (u.stem + ".o"))] for u in units]
+    # zero-filled allocations inside the module (see zeroed_new.cpp: the
+    # reference's Bloom filter reads members before they are initialised)
+    cmds.append([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-c",
+                 str(HERE / "zeroed_new.cpp"), "-o", str(OBJ / "zeroed_new.o")])
     BIN.mkdir(parents=True, exist_ok=True)
     cmds.append([nvcc, *ARCH, *FLAGS, f"-I{SHIM}", f"-I{cpp / 'include'}", f"-I{cpp / 'src'}",
                  str(HERE / "ref_fuzzy_driver.cu"), "-o", str(fuzzy_driver_path())])
@@ -146,7 +155,8 @@ def build(verbose: bool = False) -> Path | None:
 
     with ThreadPoolExecutor(max_workers=3) as ex:
         list(ex.map(run, cmds))
-    run([nvcc, *ARCH, "-shared", "-o", str(out), *[str(OBJ / (u.stem + ".o")) for u in units]])
+    run([nvcc, *ARCH, "-shared", "-o", str(out), *[str(OBJ / (u.stem + ".o")) for u in units],
+         str(OBJ / "zeroed_new.o"), "-Xlinker", f"--version-script={HERE / 'zeroed_new.map'}"])
     return out
 
 

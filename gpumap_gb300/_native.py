@@ -79,6 +79,8 @@ _SIGS = [
     ("gm_get_neighbor_indices", C.c_int, [_P, C.POINTER(gm_view)]),
     ("gm_get_neighbor_dists", C.c_int, [_P, C.POINTER(gm_view)]),
     ("gm_get_stream", C.c_int, [_P, C.POINTER(_P)]),
+    ("gm_stream_wait", C.c_int, [_P, _P]),
+    ("gm_get_device", C.c_int, [_P, C.POINTER(C.c_int32)]),
     ("gm_close", C.c_int, [_P]),
     ("gm_destroy", None, [_P]),
     ("gm_last_error", C.c_char_p, []),
@@ -86,6 +88,7 @@ _SIGS = [
     ("gm_get_stats", C.c_int, [_P, C.POINTER(gm_stats)]),
     ("gm_debug_buffer_size", C.c_int, [_P, C.c_int, C.POINTER(C.c_uint64)]),
     ("gm_debug_copy", C.c_int, [_P, C.c_int, _P, C.c_uint64]),
+    ("gm_debug_keep_tiles", C.c_int, [_P, C.c_int]),
     ("gm_debug_scalars", C.c_int, [_P, C.POINTER(C.c_int64), C.c_int]),
     ("gm_debug_update_queue", C.c_int, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
     ("gm_op_fuzzy_schedule", C.c_int,
@@ -195,6 +198,9 @@ class Session:
 
     def close(self) -> None:
         check(self._lib.gm_close(self._h))
+
+    def keep_tiles(self, on: bool) -> None:
+        check(self._lib.gm_debug_keep_tiles(self._h, 1 if on else 0))
 
     def set_stats(self, on: bool) -> None:
         check(self._lib.gm_set_stats(self._h, 1 if on else 0))

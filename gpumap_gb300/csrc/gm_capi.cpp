@@ -10,10 +10,6 @@
 #include "../../include/gpumap_gb300.h"
 #include "../../include/gpumap_gb300_ops.h"
 
-struct gm_session {
-  gm::Session *impl;
-};
-
 namespace {
 
 thread_local std::string g_last_error;
@@ -163,6 +159,17 @@ int gm_get_stream(const gm_session *s, void **stream_out) {
   return GM_OK;
 }
 
+int gm_stream_wait(const gm_session *s, void *consumer_stream) {
+  if (!s) return fail(GM_ERR_INVALID, "null session");
+  return guarded([&] { s->impl->order_after((cudaStream_t)consumer_stream); });
+}
+
+int gm_get_device(const gm_session *s, int32_t *device_out) {
+  if (!s || !device_out) return fail(GM_ERR_INVALID, "null argument");
+  *device_out = s->impl->device();
+  return GM_OK;
+}
+
 int gm_close(gm_session *s) {
   if (!s) return fail(GM_ERR_INVALID, "null session");
   return guarded([&] { s->impl->close(); });
@@ -263,6 +270,12 @@ int gm_debug_copy(const gm_session *s, int which, void *host, uint64_t bytes) {
   if (bytes == 0) return GM_OK;
   cudaStreamSynchronize(s->impl->stream());
   return ck(cudaMemcpy(host, src, bytes, cudaMemcpyDeviceToHost), "debug copy");
+}
+
+int gm_debug_keep_tiles(gm_session *s, int on) {
+  if (!s) return fail(GM_ERR_INVALID, "null session");
+  s->impl->set_keep_tile(on != 0);
+  return GM_OK;
 }
 
 int gm_debug_scalars(const gm_session *s, int64_t *out, int n) {
@@ -383,7 +396,7 @@ int gm_op_sgd(float *emb, int64_t n, const int32_t *head, const int32_t *tail,
     // scalars: iscal[0..16) at sc, fscal at sc + 64; grid-barrier words in
     // iscal[8..9], device error word in iscal[10]
     int *isc = (int *)sc;
-    const cudaError_t le = gm::launch_sgd_persistent(
+    const cudaError_t le = gm::launch_sgd_call(
         emb, head, tail, eps, (float *)ns, (float *)nn, isc, (const float *)((char *)sc + 64),
         alpha0, gamma, a, b, n_epochs, neg_rate, seed, (int *)pm, (int *)((char *)sc + 128),
         (unsigned *)(isc + gm::kIscalBarrier), (unsigned *)(isc + 10), dev, s);

@@ -51,17 +51,115 @@ int metric_from(const py::object &v) {
   return v.cast<int>();
 }
 
-py::object cai(const gm_view &v) {
-  py::dict d;
-  d["version"] = 3;
-  d["shape"] = py::make_tuple(v.rows, v.cols);
-  d["typestr"] = v.dtype == GM_DTYPE_U32 ? "<u4" : "<f4";
-  d["strides"] = py::make_tuple(v.row_stride_bytes, (uint64_t)4);
-  d["data"] = py::make_tuple(reinterpret_cast<uintptr_t>(v.ptr), true);
-  py::object ns = py::module_::import("types").attr("SimpleNamespace")();
-  ns.attr("__cuda_array_interface__") = d;
-  return ns;
+// ---- result views ---------------------------------------------------------
+// The reference returns a bare object carrying __cuda_array_interface__ v3
+// (cpp/bindings/utils/cai_wrapper.cuh:39-62: read-only, full capacity, no
+// stream, borrowing the engine's memory).  DeviceView keeps those fields and
+// adds the producing stream to the interface, plus the DLPack protocol
+// (__dlpack__ / __dlpack_device__) whose consumer stream is made to wait for
+// the session's queued work on the device.  A view holds a reference to its
+// model, so the memory stays valid while the view lives.
+
+// DLPack ABI (the data-interchange format's C structs, version 0.8 layout).
+struct DLDevice {
+  int32_t device_type;  // 2 = CUDA
+  int32_t device_id;
+};
+struct DLDataType {
+  uint8_t code;  // 1 = unsigned int, 2 = float
+  uint8_t bits;
+  uint16_t lanes;
+};
+struct DLTensor {
+  void *data;
+  DLDevice device;
+  int32_t ndim;
+  DLDataType dtype;
+  int64_t *shape;
+  int64_t *strides;  // in elements
+  uint64_t byte_offset;
+};
+struct DLManagedTensor {
+  DLTensor dl_tensor;
+  void *manager_ctx;
+  void (*deleter)(DLManagedTensor *self);
+};
+
+struct ViewCtx {
+  int64_t shape[2];
+  int64_t strides[2];
+  PyObject *owner;  // the model, kept alive while a consumer holds the tensor
+};
+
+void dl_delete(DLManagedTensor *t) {
+  auto *ctx = static_cast<ViewCtx *>(t->manager_ctx);
+  {
+    py::gil_scoped_acquire gil;
+    Py_XDECREF(ctx->owner);
+  }
+  delete ctx;
+  delete t;
 }
+
+void dl_capsule_destructor(PyObject *cap) {
+  // a capsule nobody consumed still owns its tensor
+  if (PyCapsule_IsValid(cap, "dltensor")) {
+    auto *t = static_cast<DLManagedTensor *>(PyCapsule_GetPointer(cap, "dltensor"));
+    if (t) t->deleter(t);
+  }
+}
+
+struct DeviceView {
+  gm_view v{};
+  gm_session *s = nullptr;
+  int device = 0;
+  py::object owner;
+
+  py::dict cai() const {
+    py::dict d;
+    d["version"] = 3;
+    d["shape"] = py::make_tuple(v.rows, v.cols);
+    d["typestr"] = v.dtype == GM_DTYPE_U32 ? "<u4" : "<f4";
+    d["strides"] = py::make_tuple(v.row_stride_bytes, (uint64_t)4);
+    d["data"] = py::make_tuple(reinterpret_cast<uintptr_t>(v.ptr), true);
+    void *st = nullptr;
+    check(gm_get_stream(s, &st));
+    // the values are complete on this stream; 0 would mean "no stream"
+    // (CUDA Array Interface v3), so the default stream is given as 1
+    d["stream"] = st ? reinterpret_cast<uintptr_t>(st) : (uintptr_t)1;
+    return d;
+  }
+
+  py::object dlpack(const py::object &stream) const {
+    if (!stream.is_none()) {
+      const auto h = stream.cast<intptr_t>();
+      if (h != -1) check(gm_stream_wait(s, reinterpret_cast<void *>(h)));
+    }
+    auto *ctx = new ViewCtx;
+    ctx->shape[0] = (int64_t)v.rows;
+    ctx->shape[1] = (int64_t)v.cols;
+    ctx->strides[0] = (int64_t)(v.row_stride_bytes / 4);
+    ctx->strides[1] = 1;
+    ctx->owner = owner.ptr();
+    Py_XINCREF(ctx->owner);
+    auto *t = new DLManagedTensor;
+    t->dl_tensor.data = v.ptr;
+    t->dl_tensor.device = DLDevice{2, device};
+    t->dl_tensor.ndim = 2;
+    t->dl_tensor.dtype = DLDataType{(uint8_t)(v.dtype == GM_DTYPE_U32 ? 1 : 2), 32, 1};
+    t->dl_tensor.shape = ctx->shape;
+    t->dl_tensor.strides = ctx->strides;
+    t->dl_tensor.byte_offset = 0;
+    t->manager_ctx = ctx;
+    t->deleter = dl_delete;
+    PyObject *cap = PyCapsule_New(t, "dltensor", dl_capsule_destructor);
+    if (!cap) {
+      dl_delete(t);
+      throw py::error_already_set();
+    }
+    return py::reinterpret_steal<py::object>(cap);
+  }
+};
 
 class Model {
  public:
@@ -103,20 +201,19 @@ class Model {
 
   void close() { check(gm_close(s_)); }
 
-  py::object get_embedding() const {
-    gm_view v;
-    check(gm_get_embedding(s_, &v));
-    return cai(v);
-  }
-  py::object get_neighbor_indices() const {
-    gm_view v;
-    check(gm_get_neighbor_indices(s_, &v));
-    return cai(v);
-  }
-  py::object get_neighbor_dists() const {
-    gm_view v;
-    check(gm_get_neighbor_dists(s_, &v));
-    return cai(v);
+  // which: 0 embedding, 1 neighbor indices, 2 neighbor distances
+  DeviceView view(int which, const py::object &self) const {
+    DeviceView dv;
+    const int rc = which == 0   ? gm_get_embedding(s_, &dv.v)
+                   : which == 1 ? gm_get_neighbor_indices(s_, &dv.v)
+                                : gm_get_neighbor_dists(s_, &dv.v);
+    check(rc);
+    int32_t dev = 0;
+    check(gm_get_device(s_, &dev));
+    dv.s = s_;
+    dv.device = dev;
+    dv.owner = self;
+    return dv;
   }
   uintptr_t session_ptr() const { return reinterpret_cast<uintptr_t>(s_); }
 
@@ -173,6 +270,12 @@ PYBIND11_MODULE(_core, m) {
       GM_RO("embedding_queue_size", embedding_queue_size);
 #undef GM_RO
 
+  py::class_<DeviceView>(m, "DeviceView")
+      .def_property_readonly("__cuda_array_interface__", &DeviceView::cai)
+      .def("__dlpack__", &DeviceView::dlpack, py::arg("stream") = py::none())
+      .def("__dlpack_device__", [](const DeviceView &v) { return py::make_tuple(2, v.device); })
+      .def_property_readonly("shape", [](const DeviceView &v) { return py::make_tuple(v.v.rows, v.v.cols); });
+
   py::class_<Model>(m, "GPUMAP")
       .def(py::init<const Params &>(), py::arg("config"))
       .def("initialize", &Model::initialize, py::arg("n_instances"), py::arg("n_features"))
@@ -180,8 +283,8 @@ PYBIND11_MODULE(_core, m) {
       .def("run", &Model::run, py::arg("n_jobs_insertion"), py::arg("n_jobs_update"),
            py::arg("n_jobs_embedding"))
       .def("close", &Model::close)
-      .def("get_embedding", &Model::get_embedding)
-      .def("get_neighbor_indices", &Model::get_neighbor_indices)
-      .def("get_neighbor_dists", &Model::get_neighbor_dists)
+      .def("get_embedding", [](py::object self) { return self.cast<const Model &>().view(0, self); })
+      .def("get_neighbor_indices", [](py::object self) { return self.cast<const Model &>().view(1, self); })
+      .def("get_neighbor_dists", [](py::object self) { return self.cast<const Model &>().view(2, self); })
       .def("_session_ptr", &Model::session_ptr);
 }

@@ -84,6 +84,7 @@ Session::Session(const gm_params &p) : p_(p) {
     void *ptr = nullptr;
     ck(cudaMalloc(&ptr, std::max<size_t>(bytes, 16)), "cudaMalloc");
     allocs_.push_back(ptr);
+    fixed_bytes_ += std::max<size_t>(bytes, 16);
     return ptr;
   };
   try {
@@ -143,15 +144,15 @@ Session::Session(const gm_params &p) : p_(p) {
     ck(cudaMallocHost((void **)&h_emb_pin_, (Nm + 64) * sizeof(uint32_t)), "cudaMallocHost");
     if (p.precision == 1) {
       // split-BF16 shadow rows (hi | lo, 2 x dh bf16 each) plus a block of
-      // distance / candidate scratch sized so that a block holds at most
-      // ~512 MB of each
+      // candidate / pair scratch sized so that a block holds at most ~256 MB
+      // of each (at least 128 rows)
       dh_ = exact_dh((int)d);
       xh_ = dalloc(Nm * (size_t)dh_ * 4);
-      ex_block_ = (int)std::max<size_t>(128, std::min<size_t>(4096, ((size_t)512 << 20) / (Nm * 4)));
+      ex_block_ = (int)std::max<size_t>(128, std::min<size_t>(4096, ((size_t)256 << 20) / (Nm * 4)));
       ex_block_ = ex_block_ / 128 * 128;
-      ex_D_ = (float *)dalloc((size_t)ex_block_ * Nm * sizeof(float));
+      // the approximate tile itself is only stored on request (tests), in
+      // a buffer allocated then
       ex_cand_ = (int *)dalloc((size_t)ex_block_ * Nm * sizeof(int));
-      xs_.D = ex_D_;
       xs_.cand = ex_cand_;
       xs_.cand_d = (float *)dalloc((size_t)ex_block_ * Nm * sizeof(float));
       xs_.row_cnt = (int *)dalloc((size_t)ex_block_ * sizeof(int));
@@ -159,8 +160,13 @@ Session::Session(const gm_params &p) : p_(p) {
       xs_.pool_j = (int *)dalloc((size_t)xs_.pool_cap * sizeof(int));
       xs_.pool_m = (int *)dalloc((size_t)xs_.pool_cap * sizeof(int));
       xs_.pool_d = (float *)dalloc((size_t)xs_.pool_cap * sizeof(float));
-      xs_.seg = (int *)dalloc(Nm * 2 * sizeof(int));
-      xs_.slab = (int *)dalloc(((size_t)ex_block_ / 32 + 1) * Nm * sizeof(int));
+      xs_.pool_j2 = (int *)dalloc((size_t)xs_.pool_cap * sizeof(int));
+      xs_.pool_m2 = (int *)dalloc((size_t)xs_.pool_cap * sizeof(int));
+      xs_.row_t = (float *)dalloc((size_t)ex_block_ * sizeof(float));
+      xs_.heaps = (float *)dalloc((size_t)ex_block_ * std::max(sms_, 1) * 32 * sizeof(float));
+      xs_.pcnt = (int *)dalloc((Nm + 1) * sizeof(int));
+      xs_.poff = (int *)dalloc((Nm + 1) * sizeof(int));
+      xs_.tmp = (int *)dalloc(scan_tmp_ints((int)Nm) * sizeof(int));
       xs_.counter = (int *)dalloc(16 * sizeof(int));
     }
   } catch (...) {
@@ -248,10 +254,31 @@ Session::~Session() {
   }
   if (h_pin_) cudaFreeHost(h_pin_);
   if (h_emb_pin_) cudaFreeHost(h_emb_pin_);
+  if (cstream_) cudaStreamSynchronize(cstream_);
+  for (auto &slot : ring_) {
+    if (slot.done) cudaEventDestroy(slot.done);
+    if (slot.buf) cudaFreeHost(slot.buf);
+  }
+  if (cstream_) cudaStreamDestroy(cstream_);
   release_streams();
 }
 
 void Session::sync() { ck(cudaStreamSynchronize(stream_), "cudaStreamSynchronize"); }
+
+// The consumer stream waits (on the device) for the work queued so far on
+// the main and the embedding streams; the main stream already waits for
+// every row transfer.
+void Session::order_after(cudaStream_t consumer) const {
+  for (cudaStream_t producer : {stream_, estream_}) {
+    if (!producer) continue;
+    cudaEvent_t ev = nullptr;
+    ck(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+    const cudaError_t e1 = cudaEventRecord(ev, producer);
+    const cudaError_t e2 = e1 == cudaSuccess ? cudaStreamWaitEvent(consumer, ev, 0) : e1;
+    cudaEventDestroy(ev);  // the wait keeps the recorded work
+    ck(e2, "stream wait");
+  }
+}
 
 // Waits for every phase in flight, the overlapped embedding included, and
 // reports a device error bit raised meanwhile.
@@ -288,6 +315,41 @@ void Session::ensure_cand(size_t rows) {
   ck(cudaMalloc(&cand_cnt_, r * sizeof(int)), "cudaMalloc cand");
   ck(cudaMalloc(&cand_dist_, r * kMaxCand * sizeof(float)), "cudaMalloc cand");
   cand_rows_ = r;
+}
+
+void Session::set_keep_tile(bool on) {
+  if (on && p_.precision == 1 && !ex_D_) {
+    drain();
+    const size_t bytes = (size_t)ex_block_ * std::max<size_t>(p_.n_instances, 1) * sizeof(float);
+    void *ptr = nullptr;
+    ck(cudaMalloc(&ptr, bytes), "cudaMalloc tile");
+    allocs_.push_back(ptr);
+    fixed_bytes_ += bytes;
+    ex_D_ = (float *)ptr;
+    xs_.D = ex_D_;
+  }
+  keep_tile_ = on;
+}
+
+size_t Session::device_bytes() const {
+  size_t b = fixed_bytes_;
+  b += cand_rows_ * (size_t)kMaxCand * (sizeof(int) + sizeof(float)) + cand_rows_ * sizeof(int);
+  if (es_.coo_row)
+    b += es_.cap_coo * 9 * 4 + (compact_tmp_ints((int)es_.cap_coo) + 64) * sizeof(int);
+  return b;
+}
+
+size_t Session::growth_bytes(uint32_t n_ins, uint32_t n_emb) const {
+  size_t g = 0;
+  if (p_.precision == 0 && n_ins > cand_rows_) {
+    const size_t r = std::max<size_t>(n_ins, 1024);
+    g += r * (size_t)kMaxCand * (sizeof(int) + sizeof(float)) + r * sizeof(int);
+  }
+  // an embedding batch takes the queued new rows plus the cursor's rows
+  const size_t nb = std::max<size_t>(n_emb, n_inserted_ + n_ins - emb_new_head_);
+  const size_t c = std::max<size_t>(2 * std::max<size_t>(nb, 1) * (size_t)st_.k, 4096);
+  if (n_emb > 0 && c > es_.cap_coo) g += c * 9 * 4 + (compact_tmp_ints((int)c) + 64) * sizeof(int);
+  return g;
 }
 
 void Session::ensure_embed(size_t nb) {
@@ -414,6 +476,14 @@ void Session::get_stats(gm_stats *out) {
 // ---------------------------------------------------------------------------
 // append (reference impl.cuh:77-101)
 // ---------------------------------------------------------------------------
+// Appends rows at [n_inserted, +n_rows) of X (row stride ld; reference
+// append_host, matrix_utils.cuh:50-63, a cudaMemcpy2DAsync into stride d+1).
+// Host rows go through the ingest ring: a copy stream and two pinned staging
+// slots.  Rows already in page-locked memory are copied from where they are;
+// pageable rows are first copied into the next slot (waiting only for that
+// slot's previous transfer).  The main stream waits for the transfer on the
+// device, so the host returns as soon as it is queued and the transfer of
+// the next chunk overlaps the work still running (an overlapped embedding).
 void Session::append(const float *rows, size_t n_rows, size_t n_cols, bool on_device) {
   if (closed_) throw Error(GM_ERR_CLOSED, "session is closed");
   if (n_rows == 0) return;
@@ -423,10 +493,45 @@ void Session::append(const float *rows, size_t n_rows, size_t n_cols, bool on_de
   if (n_inserted_ + n_rows > p_.n_instances)
     throw Error(GM_ERR_CAPACITY, "Exceeding maximum number of rows in storage");
   float *dst = st_.X + n_inserted_ * (size_t)st_.ld;
-  ck(cudaMemcpy2DAsync(dst, (size_t)st_.ld * sizeof(float), rows, n_cols * sizeof(float),
-                       n_cols * sizeof(float), n_rows,
-                       on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream_),
-     "append copy");
+  const size_t pitch = (size_t)st_.ld * sizeof(float), width = n_cols * sizeof(float);
+  if (on_device) {
+    ck(cudaMemcpy2DAsync(dst, pitch, rows, width, width, n_rows, cudaMemcpyDeviceToDevice, stream_),
+       "append copy");
+  } else {
+    if (!cstream_) {
+      ck(cudaStreamCreateWithFlags(&cstream_, cudaStreamNonBlocking), "cudaStreamCreate");
+      for (auto &slot : ring_) ck(cudaEventCreateWithFlags(&slot.done, cudaEventDisableTiming), "cudaEventCreate");
+    }
+    cudaPointerAttributes attr{};
+    const bool pinned = cudaPointerGetAttributes(&attr, rows) == cudaSuccess &&
+                        (attr.type == cudaMemoryTypeHost || attr.type == cudaMemoryTypeManaged);
+    cudaGetLastError();
+    RingSlot &slot = ring_[ring_next_];
+    ring_next_ = (ring_next_ + 1) % kRingSlots;
+    const float *src = rows;
+    if (!pinned) {
+      const size_t bytes = n_rows * width;
+      ck(cudaEventSynchronize(slot.done), "ingest slot");  // its previous transfer
+      if (slot.cap < bytes) {
+        if (slot.buf) cudaFreeHost(slot.buf);
+        slot.buf = nullptr;
+        slot.cap = 0;
+        ck(cudaMallocHost(&slot.buf, std::max<size_t>(bytes, (size_t)8 << 20)), "cudaMallocHost ingest");
+        slot.cap = std::max<size_t>(bytes, (size_t)8 << 20);
+      }
+      std::memcpy(slot.buf, rows, bytes);
+      src = (const float *)slot.buf;
+    }
+    ck(cudaMemcpy2DAsync(dst, pitch, src, width, width, n_rows, cudaMemcpyHostToDevice, cstream_),
+       "append copy");
+    ck(cudaEventRecord(slot.done, cstream_), "ingest event");
+    ck(cudaStreamWaitEvent(stream_, slot.done, 0), "ingest wait");
+    if (pinned) {
+      // the caller's buffer is in use until the transfer ends: block here
+      // rather than let the caller overwrite it (the slot event covers it)
+      ck(cudaEventSynchronize(slot.done), "append copy");
+    }
+  }
   n_inserted_ += n_rows;
 }
 
@@ -520,13 +625,14 @@ uint32_t Session::insert(uint32_t n_ops) {
     for (int b0 = 0; b0 < nb; b0 += ex_block_) {
       const int rows = std::min(ex_block_, nb - b0);
       timed_begin(3);
-      launch_exact_dist(st_, maps_, dh_, row0, b0, rows, ncol, ex_D_, (long)ncol, sms_, s);
+      launch_exact_dist(st_, maps_, dh_, row0, b0, rows, ncol, xs_, (long)ncol, keep_tile_, sms_, s);
       timed_end(3);
       timed_begin(4);
       launch_exact_screen(st_, row0, b0, rows, ncol, xs_, (long)ncol, sms_, s);
       timed_end(4);
-      // three BF16 products per padded feature (hi.hi, hi.lo, lo.hi)
-      const uint64_t flops = 6ull * (uint64_t)rows * (uint64_t)ncol * (uint64_t)dh_;
+      // three BF16 products per padded feature (hi.hi, hi.lo, lo.hi), two
+      // passes over the tile
+      const uint64_t flops = 12ull * (uint64_t)rows * (uint64_t)ncol * (uint64_t)dh_;
       stats_.exact_flops += (double)(stats_on_ ? flops : 0);
     }
   } else {
@@ -730,14 +836,14 @@ uint32_t Session::embed(uint32_t n_ops) {
 // ipartial its bins.
 void Session::run_sgd(cudaStream_t s) {
   if (p_.max_epoch == 0) return;
-  // overlapped: half the SMs, the other half stays free for the next
-  // cycle's distance work (the per-epoch time does not depend on it)
+  // overlapped: half the SMs, the other half stays free for the next cycle's
+  // distance work (the per-epoch time does not depend on it)
   const int max_ctas = p_.overlap ? std::max(1, sms_ / 2) : 0;
-  ck(launch_sgd_persistent(st_.emb, es_.t_row, es_.flag_tail, es_.t_val, es_.next_s, es_.next_n,
-                           es_.iscal, es_.fscal, p_.alpha, 1.0f, p_.a, p_.b, (int)p_.max_epoch,
-                           (int)p_.negative_sample_rate, 42ull, es_.t_col, es_.ipartial,
-                           (unsigned *)(es_.iscal + kIscalBarrier), st_.err, device_, s, st_.stat,
-                           max_ctas),
+  ck(launch_sgd_call(st_.emb, es_.t_row, es_.flag_tail, es_.t_val, es_.next_s, es_.next_n,
+                     es_.iscal, es_.fscal, p_.alpha, 1.0f, p_.a, p_.b, (int)p_.max_epoch,
+                     (int)p_.negative_sample_rate, 42ull, es_.t_col, es_.ipartial,
+                     (unsigned *)(es_.iscal + kIscalBarrier), st_.err, device_, s, st_.stat,
+                     max_ctas),
      "SGD launch");
 }
 

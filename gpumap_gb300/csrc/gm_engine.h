@@ -71,7 +71,15 @@ class Session {
   cudaStream_t stream() const { return stream_; }
   int device() const { return device_; }
   void set_stats(bool on) { stats_on_ = on; }
+  // device memory the session holds now, and what a run with these op
+  // counts could add (its scratch grows on demand)
+  size_t device_bytes() const;
+  size_t growth_bytes(uint32_t n_ins, uint32_t n_emb) const;
+  // keep each insertion block's approximate distance tile (tests)
+  void set_keep_tile(bool on);
   void drain();
+  // consumer waits (on the device) for everything queued on this session
+  void order_after(cudaStream_t consumer) const;
   void get_stats(gm_stats *out);
   void reset_stats();
   void debug_scalars(int64_t *out, int n) const;
@@ -105,10 +113,22 @@ class Session {
   cudaStream_t estream_ = nullptr;
   cudaEvent_t ev_pub_ = nullptr, ev_emb_ = nullptr;
   bool emb_pending_ = false;
+  // ingest ring: host-to-device row transfers on their own stream, pageable
+  // rows staged through two pinned slots
+  static constexpr int kRingSlots = 2;
+  struct RingSlot {
+    void *buf = nullptr;
+    size_t cap = 0;
+    cudaEvent_t done = nullptr;
+  };
+  cudaStream_t cstream_ = nullptr;
+  RingSlot ring_[kRingSlots];
+  int ring_next_ = 0;
   DevState st_;
   UpdScratch us_;
   EmbedScratch es_;
   std::vector<void *> allocs_;
+  size_t fixed_bytes_ = 0;
 
   // insertion candidates (grow on demand)
   int *cand_ = nullptr, *cand_cnt_ = nullptr;
@@ -137,6 +157,7 @@ class Session {
 
   // statistics
   bool stats_on_ = false;
+  bool keep_tile_ = false;
   gm_stats stats_{};
   struct EvPair { cudaEvent_t a, b; int slot; };
   std::vector<EvPair> ev_pending_;
@@ -155,3 +176,8 @@ class Session {
 };
 
 }  // namespace gm
+
+// The C ABI's opaque session handle (include/gpumap_gb300.h).
+struct gm_session {
+  gm::Session *impl;
+};

@@ -12,15 +12,21 @@
 //
 //  k_to_bf16     batch rows -> [hi | lo] shadow rows (each zero padded to dh, a multiple of 64)
 //  k_exact_dist  approx D[m][j] = |x_m|^2 + |x_j|^2 - 2 (x_m . x_j)_split
-//                (tcgen05.mma kind::f16, M=128 x N=256 x K=16 per instruction)
-//  k_exact_rows  per batch row: bound, candidates, FP32 re-score, exact top-32
-//  k_exact_cols  per existing row: batch rows that may enter its list
+//                (tcgen05.mma kind::f16, M=128 x N=256 x K=16 per instruction),
+//                screened as the accumulators are drained (the tile is not
+//                stored): per batch row, the columns that may be among its
+//                32 nearest; per existing row, the batch rows that may enter
+//                its list
+//  k_row_threshold  per batch row: its exact threshold from the CTAs' heaps
+//  k_row_dists / k_pair_dists   canonical FP32 re-score of the survivors
+//  k_row_select / k_col_merge   exact top-32 merges
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cmath>
+#include <atomic>
 #include <mutex>
 
 #include "gm_common.cuh"
@@ -42,7 +48,10 @@ constexpr int kTmemCols = 512;                 // two 128 x 256 FP32 accumulator
 constexpr uint32_t kWaitLimit = 1u << 24;      // bounded mbarrier waits
 constexpr int kStagePitch = 33;                // epilogue staging row pitch (floats)
 constexpr size_t kEpiBytes = (size_t)4 * 32 * kStagePitch * sizeof(float);
-constexpr size_t kExactSmem = (size_t)kStages * kStageBytes + 1024 + 256 + kEpiBytes;
+constexpr int kListTop = 32;                   // list width the screen keeps exact
+constexpr size_t kHeapBytes = (size_t)kListTop * kTM * sizeof(float);
+constexpr size_t kExactSmem = (size_t)kStages * kStageBytes + 1024 + 256 + kEpiBytes + kHeapBytes;
+static_assert(kExactSmem <= 232448, "k_exact_dist shared memory above the 227 KB per-CTA limit");
 
 // Instruction descriptor, kind::f16: D=F32 (bits 4-5), A=B=BF16 (7-9, 10-12),
 // both K-major (15, 16 = 0), N>>3 at 17-22, M>>4 at 24-28.
@@ -145,12 +154,84 @@ __global__ void k_to_bf16(const float *X, int ld, int d, int dh, int row0, int n
   }
 }
 
-// Approximate distances of a block of batch rows against all columns.
-// grid.y: 128-row tiles of the batch; grid.x: CTAs sharing the column tiles.
+// Rigorous bound on |approx - canonical| for one pair, as coef * sqrt(na nb)
+// + 2^-21 (na + nb), with coef from exact_bound_coef.  Both distances share
+// fl(na + nb); they differ by 2 |v - dot_c| plus the final subtraction's
+// rounding (2^-24 of |s - 2v| and of |s - 2 dot_c|, each below 2 (na + nb)
+// for any pair within the bound).  sa, sb: sqrt(na), sqrt(nb) rounded up, so
+// sa * sb (rounded up) >= sqrt(na nb).
+GM_D float pair_bound(float coef, float sa, float sb, float na, float nb) {
+  return __fadd_ru(__fmul_ru(coef, __fmul_ru(sa, sb)),
+                   __fadd_ru(__fmul_ru(4.8e-7f, __fadd_ru(na, nb)), 1e-30f));
+}
+
+
+// Max-heap of the 32 smallest upper bounds of one row, in shared memory with
+// stride kTM (element i of row r at h[i * kTM]).  Pushes x (the caller has
+// checked x < the current threshold) and returns the new threshold: the
+// largest of the 32 once the heap is full, +inf before.
+GM_D float heap_push(float *h, int &cnt, float x) {
+  if (cnt < kListTop) {
+    int pos = cnt++;
+    while (pos > 0) {
+      const int up = (pos - 1) >> 1;
+      const float pv = h[up * kTM];
+      if (pv >= x) break;
+      h[pos * kTM] = pv;
+      pos = up;
+    }
+    h[pos * kTM] = x;
+    return cnt < kListTop ? __int_as_float(0x7f800000) : h[0];
+  }
+  int pos = 0;
+  for (;;) {
+    int c = 2 * pos + 1;
+    if (c >= kListTop) break;
+    if (c + 1 < kListTop && h[(c + 1) * kTM] > h[c * kTM]) ++c;
+    const float cv = h[c * kTM];
+    if (cv <= x) break;
+    h[pos * kTM] = cv;
+    pos = c;
+  }
+  h[pos * kTM] = x;
+  return h[0];
+}
+
+// Screen state of one block of batch rows (batch-local row m).
+struct TileScreen {
+  float *heaps;       // (m * gridDim.x + CTA) * 32: each CTA's 32 smallest upper bounds of row m
+  const float *row_t; // exact per-row thresholds (pass 2)
+  int *cand;          // m * cand_ld + i: candidate columns of row m (pass 2)
+  long cand_ld;
+  int *row_cnt;       // candidates per row (zeroed before pass 2)
+  int *pool_j, *pool_m;  // (existing row, batch row) pairs that may enter j's list
+  int *pool_counter;
+  long pool_cap;
+  const Key *g_key;   // working lists (the 32nd entry of an existing row is its bar)
+  int n_exist;        // rows [0, n_exist) are the existing rows
+  float coef;
+};
+
+// Distances of a block of batch rows against all columns, screened as they
+// leave the tensor memory (the tile itself is not stored).  grid.y: 128-row
+// tiles of the batch; grid.x: CTAs sharing the column tiles.  For every pair
+// (batch row m, column j) the epilogue forms D and the bound B (pair_bound).
+//  Pass 1 (kPass == 1): every CTA keeps, per row, a max-heap of the 32
+//    smallest upper bounds D + B it sees and stores it to sc.heaps at the
+//    end; the row's 32nd smallest upper bound over all columns is the 32nd
+//    smallest of the union of those heaps (k_row_threshold).  Column side,
+//    for an existing row j: (j, m) is stored when D - B is at most the 32nd
+//    distance of j's list.
+//  Pass 2 (kPass == 2): the same tile again; j becomes a candidate of row m
+//    when D - B is at most m's exact threshold.  The candidates hold every
+//    column whose canonical distance can be among m's 32 smallest.
+// With kKeepD (pass 1 only) the tile is also written to D (ldD columns per
+// row), for tests.
+template <int kPass, bool kKeepD>
 __global__ void __launch_bounds__(kExactThreads, 1)
     k_exact_dist(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
-                 int arow0, int nb, int n, int kchunks, int dh, const float *norms, float *D,
-                 long ldD, unsigned *err) {
+                 int arow0, int nb, int n, int kchunks, int dh, const float *norms,
+                 const float *snorms, TileScreen sc, float *D, long ldD, unsigned *err) {
   extern __shared__ __align__(1024) unsigned char raw[];
   unsigned char *base = (unsigned char *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(base + (size_t)kStages * kStageBytes);
@@ -159,6 +240,7 @@ __global__ void __launch_bounds__(kExactThreads, 1)
   uint64_t *tmem_empty = tmem_full + 2;   // [2]: accumulator b has been drained
   uint32_t *tmem_slot = (uint32_t *)(tmem_empty + 2);
   float *epi = (float *)(base + (size_t)kStages * kStageBytes + 256);
+  float *heaps = (float *)((unsigned char *)epi + kEpiBytes);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int mt = blockIdx.y;
@@ -243,14 +325,23 @@ __global__ void __launch_bounds__(kExactThreads, 1)
     }
     __syncwarp();
   } else {
-    // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (tile rows); each
-    // 32 x 32 chunk is staged in shared memory (pitch 33: conflict free) and
-    // written out a row segment (128 contiguous bytes) per store
+    // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (tile rows), one row
+    // per thread, 32 columns per tcgen05.ld; column norms, bound factors and
+    // list bars are loaded one column per lane and passed by shuffles
     const int quarter = warp & 3;
     const int r = quarter * 32 + lane;
     const int m = m0 + r;
-    const float nm = m < nb ? norms[arow0 + m] : 0.0f;
+    const bool live = m < nb;
+    const int row = arow0 + m;
+    const float nm = live ? norms[row] : 0.0f;
+    const float sm = live ? snorms[row] : 0.0f;
+    const float inf = __int_as_float(0x7f800000);
     float *stg = epi + (size_t)quarter * 32 * kStagePitch;
+    float *heap = heaps + r;
+    int hcnt = 0;
+    float t_loc = inf;  // pass 1: the heap's largest once it holds 32
+    const float t_row = (kPass == 2 && live) ? sc.row_t[m] : inf;
+    int *cand_m = sc.cand + (long)m * sc.cand_ld;
     uint32_t tc = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++tc) {
       const uint32_t b = tc & 1u;
@@ -263,25 +354,64 @@ __global__ void __launch_bounds__(kExactThreads, 1)
         uint32_t v[32];
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + b * (uint32_t)kTN + (uint32_t)c, v);
         const int col0 = t * kTN + c;
-        const float njl = col0 + lane < n ? norms[col0 + lane] : 0.0f;
-#pragma unroll
+        const int jl = col0 + lane;
+        const float njl = jl < n ? norms[jl] : 0.0f;
+        const float sjl = jl < n ? snorms[jl] : 0.0f;
+        float wjl = -inf;
+        if (kPass == 1 && jl < sc.n_exist) wjl = key_dist(sc.g_key[(size_t)jl * kListW + kListW - 1]);
+#pragma unroll 4
         for (int i = 0; i < 32; ++i) {
           const float nj = __shfl_sync(0xffffffffu, njl, i);
-          stg[lane * kStagePitch + i] =
-              __fsub_rn(__fadd_rn(nm, nj), __fmul_rn(2.0f, __uint_as_float(v[i])));
-        }
-        __syncwarp();
-        if (col0 + lane < n) {
-#pragma unroll 4
-          for (int rr = 0; rr < 32; ++rr) {
-            const int mrow = m0 + quarter * 32 + rr;
-            if (mrow < nb) D[(long)mrow * ldD + col0 + lane] = stg[rr * kStagePitch + lane];
+          const float sj = __shfl_sync(0xffffffffu, sjl, i);
+          const int j = col0 + i;
+          const float dv = __fsub_rn(__fadd_rn(nm, nj), __fmul_rn(2.0f, __uint_as_float(v[i])));
+          if (kKeepD) stg[lane * kStagePitch + i] = dv;
+          const float bnd = pair_bound(sc.coef, sm, sj, nm, nj);
+          if (kPass == 1) {
+            const float wj = __shfl_sync(0xffffffffu, wjl, i);
+            if (live && j < n && j != row) {
+              const float ub = fmaxf(__fadd_ru(dv, bnd), 0.0f);
+              if (ub < t_loc) t_loc = heap_push(heap, hcnt, ub);
+            }
+            const bool hit = live && j < sc.n_exist && __fsub_rd(dv, bnd) <= wj;
+            const unsigned bal = __ballot_sync(0xffffffffu, hit);
+            if (bal) {
+              const int leader = __ffs(bal) - 1;
+              int q0 = 0;
+              if (lane == leader) q0 = atomicAdd(sc.pool_counter, __popc(bal));
+              q0 = __shfl_sync(0xffffffffu, q0, leader);
+              if (hit) {
+                const long q = (long)q0 + __popc(bal & ((1u << lane) - 1u));
+                if (q < sc.pool_cap) {
+                  sc.pool_j[q] = j;
+                  sc.pool_m[q] = m;
+                } else {
+                  atomicOr(err, kDevErrOverflow);
+                }
+              }
+            }
+          } else if (live && j < n && j != row && __fsub_rd(dv, bnd) <= t_row) {
+            cand_m[atomicAdd(&sc.row_cnt[m], 1)] = j;
           }
         }
-        __syncwarp();
+        if (kKeepD) {
+          __syncwarp();
+          if (col0 + lane < n) {
+#pragma unroll 4
+            for (int rr = 0; rr < 32; ++rr) {
+              const int mrow = m0 + quarter * 32 + rr;
+              if (mrow < nb) D[(long)mrow * ldD + col0 + lane] = stg[rr * kStagePitch + lane];
+            }
+          }
+          __syncwarp();
+        }
       }
       tc_fence_before();
       mbar_arrive(&tmem_empty[b]);
+    }
+    if (kPass == 1 && live) {
+      float *out = sc.heaps + ((size_t)m * gridDim.x + blockIdx.x) * kListTop;
+      for (int i = 0; i < kListTop; ++i) out[i] = i < hcnt ? heap[i * kTM] : inf;
     }
   }
   tc_fence_before();
@@ -293,29 +423,18 @@ __global__ void __launch_bounds__(kExactThreads, 1)
   }
 }
 
-// Rigorous bound on |approx - canonical| for one pair, as coef * sqrt(na nb)
-// + 2^-21 (na + nb), with coef from exact_bound_coef.  Both distances share
-// fl(na + nb); they differ by 2 |v - dot_c| plus the final subtraction's
-// rounding (2^-24 of |s - 2v| and of |s - 2 dot_c|, each below 2 (na + nb)
-// for any pair within the bound).  sa, sb: sqrt(na), sqrt(nb) rounded up, so
-// sa * sb (rounded up) >= sqrt(na nb).
-GM_D float pair_bound(float coef, float sa, float sb, float na, float nb) {
-  return __fadd_ru(__fmul_ru(coef, __fmul_ru(sa, sb)),
-                   __fadd_ru(__fmul_ru(4.8e-7f, __fadd_ru(na, nb)), 1e-30f));
-}
-
-// ---- screen: bound test, exact FP32 re-score, exact top-32 -----------------
+// ---- screen: exact threshold, FP32 re-score, exact top-32 -----------------
 //
-// Per block of batch rows (brow0 .. brow0 + nrows) against columns [0, n):
-//  k_row_scan    CTA per batch row: threshold T (32nd smallest upper bound),
-//                candidate columns whose lower bound reaches T
-//  k_col_*       existing rows j < n_exist: batch rows whose lower bound
-//                reaches j's current 32nd distance, as a contiguous segment
-//                of the column pool
+// Around and after k_exact_dist, per block of batch rows (brow0 .. +nrows):
+//  k_row_threshold  warp per batch row: T = 32nd smallest upper bound over all
+//                columns, from the union of the CTAs' heaps (pass 1), for the
+//                candidate test of pass 2
+//  k_pool_count / k_pool_scatter   groups the column pairs by existing row
+//                (counting sort; order inside a group is free)
 //  k_row_dists   canonical distances of the row candidates
-//  k_pair_dists  canonical distances of the column pool
+//  k_pair_dists  canonical distances of the column pairs
 //  k_row_select  warp per batch row: exact top-32 keys of its candidates
-//  k_col_merge   thread per existing row: merges its segment into its list
+//  k_col_merge   warp per existing row: merges its pairs into its list
 // Both merges are order independent: a list ends as the 32 smallest keys of
 // its old entries and every candidate, and keys are unique (distinct ids).
 //
@@ -325,159 +444,61 @@ GM_D float pair_bound(float coef, float sa, float sb, float na, float nb) {
 // reads tile row l at column i: bank (l * 33 + i) mod 32, conflict free).
 // fmaf(a, b, c) = fmaf(b, a, c) exactly, so d(x, y) = d(y, x) bit for bit.
 
-constexpr int kScanThreads = 256;
 constexpr int kTile = 32;
 constexpr int kTileLd = 33;
+constexpr int kFinalWarps = 4;
 
-GM_D unsigned block_sum(unsigned v, unsigned *red) {
-  v = __reduce_add_sync(0xffffffffu, v);
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  unsigned t = 0;
-  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += red[i];
-  return t;
-}
-
-__global__ void __launch_bounds__(kScanThreads)
-    k_row_scan(const float *D, long ldD, int brow0, int n, const float *norms,
-               const float *snorms, float coef, int *cand, long cand_ld, int *row_cnt,
-               unsigned long long *stat) {
-  __shared__ unsigned red[kScanThreads / 32];
-  __shared__ int s_cnt;
-  const int ml = blockIdx.x, row = brow0 + ml, tid = threadIdx.x, lane = tid & 31;
-  const float nm = norms[row], sm = snorms[row];
-  const float *Dr = D + (long)ml * ldD;
+__global__ void __launch_bounds__(kFinalWarps * 32)
+    k_row_threshold(const float *heaps, int ncta, int nrows, int n, float *row_t,
+                    unsigned long long *stat) {
+  const int lane = threadIdx.x & 31;
+  const int ml = blockIdx.x * kFinalWarps + (threadIdx.x >> 5);
+  if (ml >= nrows) return;
   const float inf = __int_as_float(0x7f800000);
-  float u0 = inf, u1 = inf, u2 = inf, u3 = inf;  // this thread's 4 smallest upper bounds
-  for (int j = tid; j < n; j += kScanThreads) {
-    if (j == row) continue;
-    const float x =
-        fmaxf(__fadd_ru(Dr[j], pair_bound(coef, sm, snorms[j], nm, norms[j])), 0.0f);
-    if (x < u3) {
-      u3 = x;
-      if (u3 < u2) { const float t = u2; u2 = u3; u3 = t; }
-      if (u2 < u1) { const float t = u1; u1 = u2; u2 = t; }
-      if (u1 < u0) { const float t = u0; u0 = u1; u1 = t; }
+  const float *h = heaps + (size_t)ml * ncta * kListTop;
+  const int cnt = ncta * kListTop;
+  // the 32 smallest upper bounds of the union, ascending across the lanes
+  float top = inf;
+  for (int c0 = 0; c0 < cnt; c0 += 32) {
+    const float u = c0 + lane < cnt ? h[c0 + lane] : inf;
+    unsigned pend = __ballot_sync(0xffffffffu, u < __shfl_sync(0xffffffffu, top, 31));
+    while (pend) {
+      const int src = __ffs(pend) - 1;
+      pend &= pend - 1;
+      const float x = __shfl_sync(0xffffffffu, u, src);
+      const unsigned pos_mask = __ballot_sync(0xffffffffu, x < top);
+      if (!pos_mask) continue;
+      const int pos = __ffs(pos_mask) - 1;
+      const float prev = __shfl_up_sync(0xffffffffu, top, 1);
+      if (lane > pos) top = prev;
+      else if (lane == pos) top = x;
     }
   }
-  // T = 32nd smallest of the block's values: at least 32 distinct columns have
-  // upper bounds (so canonical distances) at or below it.  Nonnegative floats
-  // order as their bit patterns: binary-search the smallest such pattern.
-  unsigned lo = 0u, hi = 0x7f800000u;
-  const unsigned b0 = __float_as_uint(u0), b1 = __float_as_uint(u1), b2 = __float_as_uint(u2),
-                 b3 = __float_as_uint(u3);
-  while (lo < hi) {
-    const unsigned mid = lo + ((hi - lo) >> 1);
-    const unsigned c = (unsigned)(b0 <= mid) + (unsigned)(b1 <= mid) + (unsigned)(b2 <= mid) +
-                       (unsigned)(b3 <= mid);
-    if (block_sum(c, red) >= 32u) hi = mid;
-    else lo = mid + 1u;
-  }
-  const float T = n - 1 < 32 ? inf : __uint_as_float(hi);  // fewer than 32 others: all
-  if (tid == 0) s_cnt = 0;
-  __syncthreads();
-  int *cl = cand + (long)ml * cand_ld;
-  for (int j0 = 0; j0 < n; j0 += kScanThreads) {
-    const int j = j0 + tid;
-    const bool keep = j < n && j != row &&
-                      __fsub_rd(Dr[j], pair_bound(coef, sm, snorms[j], nm, norms[j])) <= T;
-    const unsigned bal = __ballot_sync(0xffffffffu, keep);
-    int base = 0;
-    if (lane == 0 && bal) base = atomicAdd(&s_cnt, __popc(bal));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (keep) cl[base + __popc(bal & ((1u << lane) - 1u))] = j;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    row_cnt[ml] = s_cnt;
-    if (stat) {
-      atomicAdd(&stat[5], (unsigned long long)n);
-      atomicAdd(&stat[6], (unsigned long long)s_cnt);
-    }
+  const float T = __shfl_sync(0xffffffffu, top, 31);
+  if (lane == 0) {
+    // fewer than 32 other rows: every column is a candidate
+    row_t[ml] = n - 1 < kListTop ? inf : T;
+    if (stat) atomicAdd(&stat[5], (unsigned long long)n);
   }
 }
 
-// Column direction in three steps over slabs of kSlab batch rows:
-//  k_col_count  thread per (existing row j, slab): hits of the bound test
-//  k_col_place  thread per j: total, a contiguous pool segment (one atomic),
-//               per-slab offsets
-//  k_col_write  thread per (j, slab): the same test again, pairs written
-// The two passes evaluate the identical test on identical inputs.
-constexpr int kSlab = 32;
-GM_D bool col_hit(const float *D, long ldD, int j, int ml, float w, float coef, float sj, float nj,
-                  float sm, float nm) {
-  return __fsub_rd(D[(long)ml * ldD + j], pair_bound(coef, sj, sm, nj, nm)) <= w;
+__global__ void k_pool_count(const int *pool_j, const int *counter, long pool_cap, int *pcnt,
+                             unsigned long long *stat) {
+  const long total = min((long)*counter, pool_cap);
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x)
+    atomicAdd(&pcnt[pool_j[e]], 1);
+  if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stat[6], (unsigned long long)total);
 }
-__global__ void __launch_bounds__(kScanThreads)
-    k_col_count(const float *D, long ldD, int n_exist, int brow0, int nrows, const float *norms,
-                const float *snorms, float coef, const Key *g_key, int *slab_cnt) {
-  __shared__ float s_n[kSlab], s_s[kSlab];
-  const int sl = blockIdx.y, m0 = sl * kSlab, mr = min(kSlab, nrows - m0);
-  if (threadIdx.x < mr) {
-    s_n[threadIdx.x] = norms[brow0 + m0 + threadIdx.x];
-    s_s[threadIdx.x] = snorms[brow0 + m0 + threadIdx.x];
-  }
-  __syncthreads();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n_exist) return;
-  const float w = key_dist(g_key[(size_t)j * kListW + kListW - 1]);
-  const float nj = norms[j], sj = snorms[j];
-  int cnt = 0;
-#pragma unroll 8
-  for (int i = 0; i < mr; ++i) cnt += col_hit(D, ldD, j, m0 + i, w, coef, sj, nj, s_s[i], s_n[i]);
-  slab_cnt[(size_t)sl * n_exist + j] = cnt;
-}
-__global__ void k_col_place(int n_exist, int nslabs, int *slab_cnt, long pool_cap, int *seg,
-                            int *counter, unsigned *err, unsigned long long *stat) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n_exist) return;
-  int tot = 0;
-  for (int sl = 0; sl < nslabs; ++sl) tot += slab_cnt[(size_t)sl * n_exist + j];
-  int base = 0;
-  if (tot) {
-    base = atomicAdd(counter, tot);
-    if ((long)base + tot > pool_cap) {
-      atomicOr(err, kDevErrOverflow);
-      tot = 0;
-      base = -1;  // nothing is written for this row
-    } else if (stat) {
-      atomicAdd(&stat[6], (unsigned long long)tot);
-    }
-  }
-  // slab counts become slab offsets (-1: skip)
-  int off = base;
-  for (int sl = 0; sl < nslabs; ++sl) {
-    const int c = slab_cnt[(size_t)sl * n_exist + j];
-    slab_cnt[(size_t)sl * n_exist + j] = base < 0 ? -1 : off;
-    off += c;
-  }
-  seg[2 * j] = base < 0 ? 0 : base;
-  seg[2 * j + 1] = tot;
-}
-__global__ void __launch_bounds__(kScanThreads)
-    k_col_write(const float *D, long ldD, int n_exist, int brow0, int nrows, const float *norms,
-                const float *snorms, float coef, const Key *g_key, const int *slab_off,
-                int *pool_j, int *pool_m) {
-  __shared__ float s_n[kSlab], s_s[kSlab];
-  const int sl = blockIdx.y, m0 = sl * kSlab, mr = min(kSlab, nrows - m0);
-  if (threadIdx.x < mr) {
-    s_n[threadIdx.x] = norms[brow0 + m0 + threadIdx.x];
-    s_s[threadIdx.x] = snorms[brow0 + m0 + threadIdx.x];
-  }
-  __syncthreads();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n_exist) return;
-  int q = slab_off[(size_t)sl * n_exist + j];
-  if (q < 0) return;
-  const float w = key_dist(g_key[(size_t)j * kListW + kListW - 1]);
-  const float nj = norms[j], sj = snorms[j];
-  for (int i = 0; i < mr; ++i) {
-    if (col_hit(D, ldD, j, m0 + i, w, coef, sj, nj, s_s[i], s_n[i])) {
-      pool_j[q] = j;
-      pool_m[q] = m0 + i;
-      ++q;
-    }
+// pcnt: zeroed again before this launch (it serves as the fill cursor)
+__global__ void k_pool_scatter(const int *pool_j, const int *pool_m, const int *counter,
+                               long pool_cap, const int *poff, int *pcnt, int *pool_j2,
+                               int *pool_m2) {
+  const long total = min((long)*counter, pool_cap);
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const int j = pool_j[e];
+    const int q = poff[j] + atomicAdd(&pcnt[j], 1);
+    pool_j2[q] = j;
+    pool_m2[q] = pool_m[e];
   }
 }
 
@@ -608,7 +629,8 @@ __global__ void __launch_bounds__(kRowDistWarps * 32)
 
 constexpr int kRowWarps = 4;
 __global__ void k_row_select(const float *cand_d, int brow0, int nrows, const int *cand,
-                             long cand_ld, const int *row_cnt, Key *g_key) {
+                             long cand_ld, const int *row_cnt, Key *g_key,
+                             unsigned long long *stat) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ml = blockIdx.x * kRowWarps + warp;
   if (ml >= nrows) return;
@@ -631,17 +653,18 @@ __global__ void k_row_select(const float *cand_d, int brow0, int nrows, const in
     }
   }
   g_key[(size_t)(brow0 + ml) * kListW + lane] = mine;
+  if (stat && lane == 0) atomicAdd(&stat[6], (unsigned long long)cnt);
 }
 
 // Warp per existing row j with pairs: lane l holds entry l of j's sorted list;
 // each new key is inserted by a ballot on the lanes whose entry it precedes.
 constexpr int kMergeWarps = 8;
-__global__ void k_col_merge(int n_exist, int brow0, const int *seg, const int *pool_m,
+__global__ void k_col_merge(int n_exist, int brow0, const int *poff, const int *pool_m,
                             const float *pool_d, Key *g_key, int *dirty) {
   const int lane = threadIdx.x & 31;
   const int j = blockIdx.x * kMergeWarps + (threadIdx.x >> 5);
   if (j >= n_exist) return;
-  const int base = seg[2 * j], cnt = seg[2 * j + 1];
+  const int base = poff[j], cnt = poff[j + 1] - poff[j];
   if (!cnt) return;
   Key *lst = g_key + (size_t)j * kListW;
   Key mine = lst[lane];
@@ -737,70 +760,96 @@ void launch_to_bf16(const DevState &st, void *xh, int dh, int row0, int nrows, c
   note_launch();
 }
 
-void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
-                       int nrows, int n, float *D, long ldD, int sms, cudaStream_t s) {
-  if (nrows <= 0 || n <= 0) return;
-  static unsigned configured = 0u;
+template <int kPass, bool kKeepD>
+static void launch_tile(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
+                        int nrows, int n, const ExactScreen &x, long ldD, int gx, int m_tiles,
+                        cudaStream_t s) {
+  // once per device (sessions on several host threads may launch at once)
+  static std::atomic<unsigned> configured{0u};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 32 && !(configured & (1u << dev))) {
-    cudaFuncSetAttribute(k_exact_dist, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (dev < 32 && !(configured.load() & (1u << dev))) {
+    cudaFuncSetAttribute(k_exact_dist<kPass, kKeepD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)kExactSmem);
-    configured |= (1u << dev);
+    configured.fetch_or(1u << dev);
   }
-  const int m_tiles = cdiv(nrows, kTM);
-  const int n_tiles = cdiv(n, kTN);
-  const int gx = std::max(1, std::min(n_tiles, std::max(1, sms / m_tiles)));
   CUtensorMap ta, tb;
   memcpy(&ta, maps.a, sizeof(ta));
   memcpy(&tb, maps.b, sizeof(tb));
-  k_exact_dist<<<dim3(gx, m_tiles), kExactThreads, kExactSmem, s>>>(
-      ta, tb, row0 + blk0, nrows, n, dh / kTK, dh, st.norms, D, ldD, st.err);
+  TileScreen sc;
+  sc.heaps = x.heaps;
+  sc.row_t = x.row_t;
+  sc.cand = x.cand;
+  sc.cand_ld = ldD;
+  sc.row_cnt = x.row_cnt;
+  sc.pool_j = x.pool_j;
+  sc.pool_m = x.pool_m;
+  sc.pool_counter = x.counter;
+  sc.pool_cap = x.pool_cap;
+  sc.g_key = st.g_key;
+  sc.n_exist = row0;
+  sc.coef = exact_bound_coef(st.d, dh);
+  k_exact_dist<kPass, kKeepD><<<dim3(gx, m_tiles), kExactThreads, kExactSmem, s>>>(
+      ta, tb, row0 + blk0, nrows, n, dh / kTK, dh, st.norms, st.snorms, sc, x.D, ldD, st.err);
   note_launch();
+}
+
+void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
+                       int nrows, int n, const ExactScreen &x, long ldD, bool keep_d, int sms,
+                       cudaStream_t s) {
+  if (nrows <= 0 || n <= 0) return;
+  const int m_tiles = cdiv(nrows, kTM);
+  const int n_tiles = cdiv(n, kTN);
+  const int gx = std::max(1, std::min(n_tiles, std::max(1, sms / m_tiles)));
+  cudaMemsetAsync(x.row_cnt, 0, (size_t)nrows * sizeof(int), s);
+  cudaMemsetAsync(x.counter, 0, sizeof(int), s);
+  if (keep_d && x.D)
+    launch_tile<1, true>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, s);
+  else
+    launch_tile<1, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, s);
+  k_row_threshold<<<cdiv(nrows, kFinalWarps), kFinalWarps * 32, 0, s>>>(x.heaps, gx, nrows, n, x.row_t,
+                                                                        st.stat);
+  note_launch();
+  launch_tile<2, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, s);
 }
 
 void launch_exact_screen(const DevState &st, int row0, int blk0, int nrows, int n,
                          const ExactScreen &x, long ldD, int sms, cudaStream_t s) {
   if (nrows <= 0 || n <= 0) return;
   const int brow0 = row0 + blk0;  // global first row of the block
-  const float coef = exact_bound_coef(st.d, exact_dh(st.d));
-  k_row_scan<<<nrows, kScanThreads, 0, s>>>(x.D, ldD, brow0, n, st.norms, st.snorms, coef,
-                                            x.cand, ldD, x.row_cnt, st.stat);
-  note_launch();
+  const int grid = 4 * std::max(sms, 1);
   if (row0 > 0) {
-    cudaMemsetAsync(x.counter, 0, sizeof(int), s);
-    const int nslabs = cdiv(nrows, kSlab);
-    const dim3 g2(cdiv(row0, kScanThreads), nslabs);
-    k_col_count<<<g2, kScanThreads, 0, s>>>(x.D, ldD, row0, brow0, nrows, st.norms, st.snorms,
-                                            coef, st.g_key, x.slab);
-    k_col_place<<<cdiv(row0, kScanThreads), kScanThreads, 0, s>>>(
-        row0, nslabs, x.slab, x.pool_cap, x.seg, x.counter, st.err, st.stat);
-    k_col_write<<<g2, kScanThreads, 0, s>>>(x.D, ldD, row0, brow0, nrows, st.norms, st.snorms,
-                                            coef, st.g_key, x.slab, x.pool_j, x.pool_m);
-    note_launch(3);
+    cudaMemsetAsync(x.pcnt, 0, (size_t)row0 * sizeof(int), s);
+    k_pool_count<<<grid, 256, 0, s>>>(x.pool_j, x.counter, x.pool_cap, x.pcnt, st.stat);
+    note_launch();
+    exclusive_scan(x.pcnt, x.poff, row0, x.tmp, s);
+    cudaMemsetAsync(x.pcnt, 0, (size_t)row0 * sizeof(int), s);
+    k_pool_scatter<<<grid, 256, 0, s>>>(x.pool_j, x.pool_m, x.counter, x.pool_cap, x.poff, x.pcnt,
+                                        x.pool_j2, x.pool_m2);
+    note_launch();
   }
-  static unsigned pair_configured = 0u;
+  static std::atomic<unsigned> pair_configured{0u};
   {
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev < 32 && !(pair_configured & (1u << dev))) {
+    if (dev < 32 && !(pair_configured.load() & (1u << dev))) {
       cudaFuncSetAttribute(k_row_dists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRowSmem);
       cudaFuncSetAttribute(k_pair_dists, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPairSmem);
-      pair_configured |= (1u << dev);
+      pair_configured.fetch_or(1u << dev);
     }
   }
   k_row_dists<<<nrows, kRowDistWarps * 32, kRowSmem, s>>>(st.X, st.ld, st.d, st.norms, brow0,
                                                          x.cand, ldD, x.row_cnt, x.cand_d);
   note_launch();
   k_row_select<<<cdiv(nrows, kRowWarps), kRowWarps * 32, 0, s>>>(x.cand_d, brow0, nrows, x.cand,
-                                                                 ldD, x.row_cnt, st.g_key);
+                                                                 ldD, x.row_cnt, st.g_key, st.stat);
   note_launch();
   if (row0 > 0) {
-    k_pair_dists<<<4 * std::max(sms, 1), kPairWarps * 32, kPairSmem, s>>>(
-        st.X, st.ld, st.d, st.norms, brow0, x.pool_j, x.pool_m, x.pool_d, x.counter, x.pool_cap);
+    k_pair_dists<<<grid, kPairWarps * 32, kPairSmem, s>>>(
+        st.X, st.ld, st.d, st.norms, brow0, x.pool_j2, x.pool_m2, x.pool_d, x.counter, x.pool_cap);
     note_launch();
     k_col_merge<<<cdiv(row0, kMergeWarps), kMergeWarps * 32, 0, s>>>(
-        row0, brow0, x.seg, x.pool_m, x.pool_d, st.g_key, st.dirty);
+        row0, brow0, x.poff, x.pool_m2, x.pool_d, st.g_key, st.dirty);
     note_launch();
   }
 }

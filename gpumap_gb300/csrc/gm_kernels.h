@@ -104,25 +104,33 @@ struct ExactMaps {
 int exact_dh(int d);  // shadow row width: d rounded up to 64
 bool make_row_maps(void *xh, int n_cap, int dh, ExactMaps *out);
 void launch_to_bf16(const DevState &st, void *xh, int dh, int row0, int nrows, cudaStream_t s);
-// Approximate distances D (nrows x ldD) of batch rows [row0+blk0, +nrows)
-// against rows [0, n) on the tensor cores.
-void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
-                       int nrows, int n, float *D, long ldD, int sms, cudaStream_t s);
-// Screen scratch of one block of batch rows (capacity rows x n_cap each).
+// Screen scratch of one block of batch rows (rows x n_cap where noted).
 struct ExactScreen {
-  float *D = nullptr;     // rows x ldD approximate distances
-  int *cand = nullptr;    // rows x ldD candidate columns per batch row
-  float *cand_d = nullptr;  // rows x ldD their canonical distances
-  int *row_cnt = nullptr; // rows candidate counts
-  int *pool_j = nullptr, *pool_m = nullptr;  // column-direction pairs
-  float *pool_d = nullptr;
-  int *seg = nullptr;     // n_cap x 2: (first pair, pairs) per existing row
-  int *slab = nullptr;    // (rows / 32 + 1) x n_cap per-slab counts, then offsets
-  int *counter = nullptr; // pairs in the pool
+  float *D = nullptr;         // rows x ldD approximate distances (written only when kept)
+  int *cand = nullptr;        // rows x ldD candidate columns per batch row
+  float *cand_d = nullptr;    // rows x ldD: their approximate, then canonical distances
+  int *row_cnt = nullptr;     // rows candidate counts
+  float *heaps = nullptr;     // rows x CTAs x 32: per-CTA smallest upper bounds (pass 1)
+  float *row_t = nullptr;     // rows exact thresholds
+  int *pool_j = nullptr, *pool_m = nullptr;    // column pairs as found
+  int *pool_j2 = nullptr, *pool_m2 = nullptr;  // grouped by existing row
+  float *pool_d = nullptr;    // their canonical distances
+  int *pcnt = nullptr;        // n_cap + 1 pairs per existing row, then fill cursors
+  int *poff = nullptr;        // n_cap + 1 group offsets
+  int *tmp = nullptr;         // scan scratch, scan_tmp_ints(n_cap)
+  int *counter = nullptr;     // pairs in the pool
   long pool_cap = 0;
 };
-// Exact lists of those rows (bound, FP32 re-score, top-32) and their offers to
-// rows [0, row0).
+// Distances of batch rows [row0+blk0, +nrows) against rows [0, n) on the
+// tensor cores, screened as the accumulators drain, in two passes (the
+// per-row exact threshold, then the candidates): candidate columns per batch
+// row and (existing row, batch row) pairs land in x.  With keep_d the
+// approximate tile is also written to x.D (nrows x ldD), for tests.
+void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
+                       int nrows, int n, const ExactScreen &x, long ldD, bool keep_d, int sms,
+                       cudaStream_t s);
+// Exact lists of those rows (threshold, FP32 re-score, top-32) and their
+// offers to rows [0, row0).
 void launch_exact_screen(const DevState &st, int row0, int blk0, int nrows, int n,
                          const ExactScreen &x, long ldD, int sms, cudaStream_t s);
 
@@ -208,6 +216,13 @@ cudaError_t launch_sgd_persistent(float *emb, const int *head, const int *tail,
                                   uint64_t seed, int *perm, int *bins, unsigned *bar,
                                   unsigned *err, int device, cudaStream_t s,
                                   unsigned long long *stat = nullptr, int max_ctas = 0);
+// One embedding call's SGD (all epochs): launch_sgd_persistent.
+cudaError_t launch_sgd_call(float *emb, const int *head, const int *tail, const float *eps,
+                            float *next_s, float *next_n, const int *iscal, const float *fscal,
+                            float alpha0, float gamma, float a, float b, int n_epochs, int neg_rate,
+                            uint64_t seed, int *perm, int *bins, unsigned *bar, unsigned *err,
+                            int device, cudaStream_t s, unsigned long long *stat = nullptr,
+                            int max_ctas = 0);
 void launch_set_int(int *p, int v, cudaStream_t s);
 constexpr int kIscalN = 4;
 constexpr int kIscalBarrier = 8;  // iscal[8..9]: SGD grid-barrier words

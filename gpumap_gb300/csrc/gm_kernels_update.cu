@@ -1,6 +1,8 @@
 // Update phase: one NN-Descent local-join round over a batch of rows.
 // Restates the reference's UpdateAlgo (update_kernel.cuh:689-1054) with the
 // sampling, reverse lists, merge and publish all on the device.
+#include <mutex>
+
 #include "gm_common.cuh"
 #include "gm_kernels.h"
 
@@ -487,19 +489,25 @@ void launch_local_join(const DevState &st, const UpdScratch &u, const int *join_
                        const int *n_join_dev, int n_join_max, int n, cudaStream_t s) {
   if (n_join_max <= 0) return;
   const size_t smem = sizeof(LJSmem);
-  static unsigned configured = 0u;  // one bit per device ordinal
+  // per device, once (sessions on several host threads may launch at once)
+  static std::mutex mu;
   static int ctas[32] = {0};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 32 && !(configured & (1u << dev))) {
-    cudaFuncSetAttribute(k_local_join, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int sms = 0, per_sm = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local_join, kLJThreads, smem);
-    ctas[dev] = std::max(1, sms * std::max(per_sm, 1));
-    configured |= (1u << dev);
+  int grid_ctas = 0;
+  if (dev < 32) {
+    std::lock_guard<std::mutex> g(mu);
+    if (!ctas[dev]) {
+      cudaFuncSetAttribute(k_local_join, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      int sms = 0, per_sm = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_local_join, kLJThreads, smem);
+      ctas[dev] = std::max(1, sms * std::max(per_sm, 1));
+    }
+    grid_ctas = ctas[dev];
   }
-  const int grid = std::min(n_join_max, dev < 32 ? ctas[dev] : 1024);
+
+  const int grid = std::min(n_join_max, grid_ctas > 0 ? grid_ctas : 1024);
   k_local_join<<<grid, kLJThreads, smem, s>>>(
       join_nodes, n_join_dev, u.fwd_new, u.fwd_old, u.rev_new, u.rev_old, u.sizes, st.X,
       st.norms, st.ld, st.d, n, st.k, st.g_key, st.locks, st.dirty, st.err, st.stat);

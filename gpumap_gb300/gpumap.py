@@ -5,12 +5,10 @@
 ``run(target_latency)`` (budget split by a strategy) or
 ``run_with_n_ops(i, u, e)`` (explicit op counts).  Results are zero-copy
 device views sliced to the inserted rows: a CuPy array when CuPy is
-installed, else a torch tensor, else the raw ``__cuda_array_interface__``
-object.
+installed, else a torch tensor (through DLPack, ordered after the session's
+queued work on torch's current stream), else the engine's view object.
 """
 from __future__ import annotations
-
-import types
 
 import numpy as np
 from scipy.optimize import curve_fit
@@ -35,23 +33,22 @@ def find_ab_params(spread, min_dist):
     return params[0], params[1]
 
 
-def _device_array(cai_obj):
+def _device_array(view):
+    """A device array over an engine view: CuPy through the CUDA Array
+    Interface when CuPy is installed, else a torch tensor through DLPack (the
+    view makes torch's current stream wait for the session's queued work),
+    else the view itself.  The memory stays the engine's."""
     try:
         import cupy as cp  # noqa: F401
 
-        return cp.asarray(cai_obj)
+        return cp.asarray(view)
     except ImportError:
         pass
     try:
         import torch
     except ImportError:
-        return cai_obj
-    # torch does not take read-only interfaces; hand it a writable-flagged
-    # copy of the same description (the memory is the engine's either way).
-    iface = dict(cai_obj.__cuda_array_interface__)
-    iface["data"] = (iface["data"][0], False)
-    holder = types.SimpleNamespace(__cuda_array_interface__=iface)
-    return torch.as_tensor(holder, device="cuda")
+        return view
+    return torch.from_dlpack(view)
 
 
 class GPUMAP:

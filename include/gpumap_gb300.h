@@ -141,6 +141,18 @@ int gm_get_neighbor_dists(const struct gm_session *s, gm_view *out);
 /* The session's CUDA stream (cudaStream_t) for stream-aware consumers. */
 int gm_get_stream(const struct gm_session *s, void **stream_out);
 
+/* Makes `consumer_stream` (a cudaStream_t; NULL is the legacy default
+ * stream) wait on the device for every piece of work the session has
+ * queued so far, on all of its streams, without blocking the host: reads of
+ * the result views issued on that stream afterwards see the finished
+ * values.  No counterpart in the reference, whose views carry no stream
+ * (cpp/bindings/utils/cai_wrapper.cuh:39-62); the DLPack export of the
+ * Python views calls it with the consumer's stream. */
+int gm_stream_wait(const struct gm_session *s, void *consumer_stream);
+
+/* The CUDA device the session's memory lives on. */
+int gm_get_device(const struct gm_session *s, int32_t *device_out);
+
 /* Replaces GPUMAP::close (impl.cuh:502-507). */
 int gm_close(struct gm_session *s);
 

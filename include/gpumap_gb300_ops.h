@@ -34,13 +34,17 @@ extern "C" {
 #define GM_BUF_PUB_IDX 15    /* n_instances x (k+1) uint32 published indices (neighbor_indices) */
 #define GM_BUF_PUB_DIST 16   /* n_instances x (k+1) float published distances (neighbor_dists) */
 #define GM_BUF_EMBEDDING 17  /* n_instances x 2 float embedding */
-#define GM_BUF_EXACT_D 18    /* precision 1: approximate distances of the last insertion block,
+#define GM_BUF_EXACT_D 18    /* precision 1, while gm_debug_keep_tiles is on: approximate distances of the last insertion block,
                                 block rows x (rows inserted so far), row-major */
 
 /* Size in bytes of internal buffer `which`. */
 int gm_debug_buffer_size(const struct gm_session *s, int which, uint64_t *bytes);
 /* Copies `bytes` bytes of internal buffer `which` to host memory. */
 int gm_debug_copy(const struct gm_session *s, int which, void *host, uint64_t bytes);
+/* Precision 1: keep (on != 0) or stop keeping each insertion block's
+ * approximate distance tile for GM_BUF_EXACT_D.  Off by default: the screen
+ * runs as the tile leaves the tensor memory and the tile is not stored. */
+int gm_debug_keep_tiles(struct gm_session *s, int on);
 /* Host and device scalars, out[0..n):
  *  0 n_inserted, 1 insertion-queue head, 2 new-row embedding-queue head,
  *  3 embedding cursor (-1 = none), 4 embedding sweeps, 5 last nnz,
@@ -81,7 +85,12 @@ int gm_op_sgd(float *emb, int64_t n, const int32_t *head, const int32_t *tail,
  * allocate while they run: a host framework whose memory pool owns the GPU
  * (a cudaMalloc beside it can fail or fragment that pool) or a latency-bound
  * loop that cannot take cudaFree's device-wide synchronisation.  No
- * counterpart in the reference.  Same arguments and results as gm_op_sgd.
+ * counterpart in the reference.  Same arguments as gm_op_sgd and the same
+ * arithmetic per edge, but one kernel launch per epoch instead of
+ * gm_op_sgd's single launch for all epochs: results equal gm_op_sgd's bit
+ * for bit where no two edges of an epoch touch the same row (and for a single
+ * edge, negative samples included); with Hogwild races they agree
+ * statistically, as two runs of either operator do.
  *  - Scratch is one fixed device array of 8 MiB + 128 bytes inside this
  *    library, held by every GPU that loads it until the process exits;
  *    nnz above GM_SGD_NOALLOC_MAX_EDGES is rejected with GM_ERR_INVALID.

@@ -50,3 +50,27 @@ def test_clock_summary_reports_throttle_reasons():
                  ["2055", "2070", "950", "Not Active", "Not Active", "Not Active", "Not Active"]]
     s = c.summary()
     assert s["sm_max_mhz"] == 2070.0 and s["reasons"] == ["sw_power_cap"] and s["samples"] == 2
+
+
+def test_embed_quality_matches_oracle_trustworthiness():
+    # both spaces restricted to the subset: with every row in it, the score is
+    # the plain trustworthiness the oracle computes
+    import torch
+
+    from oracle.knn import trustworthiness
+
+    rng = np.random.default_rng(5)
+    X = rng.normal(size=(300, 12)).astype(np.float32)
+    E = (X[:, :2] + 0.3 * rng.normal(size=(300, 2))).astype(np.float32)
+    t, kp = bench.embed_quality(torch.from_numpy(X), E, np.arange(300), k=10)
+    assert abs(t - trustworthiness(X, E, 10)) < 1e-12
+    assert 0.0 < kp <= 1.0
+    # an embedding that keeps the input itself preserves every neighbour
+    t2, kp2 = bench.embed_quality(torch.from_numpy(X[:, :2].copy()), X[:, :2].copy(), np.arange(300), k=10)
+    assert t2 == 1.0 and kp2 == 1.0
+
+
+def test_fp64_baseline_counts_rows():
+    X = np.random.default_rng(1).normal(size=(3000, 16)).astype(np.float32)
+    v, rows, dt = bench.fp64_bruteforce_baseline(X, k=5, target_s=0.0, block=512)
+    assert rows == 512 and v > 0 and dt >= 0

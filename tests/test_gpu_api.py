@@ -112,3 +112,44 @@ def test_overlap_through_python_api(precision):
     assert torch.equal(a.get_neighbor_dists(), b.get_neighbor_dists())
     a.close()
     b.close()
+
+
+def test_views_carry_stream_and_dlpack():
+    # the views keep the reference's interface (read-only CAI v3, full
+    # capacity, k+1 columns) and add the producing stream and DLPack; a
+    # consumer on another stream is ordered after the session's work
+    import torch
+
+    from gpumap_gb300 import _core
+    from gpumap_gb300.datasets import gaussian_mixture
+
+    n, d, k = 2000, 16, 10
+    X, _ = gaussian_mixture(n, d, seed=4)
+    p = _core.GPUMAPParams()
+    p.n_instances, p.n_features, p.n_neighbors, p.max_epoch = n, d, k, 30
+    p.precision, p.overlap = 1, 1
+    core = _core.GPUMAP(p)
+    core.append_data(X)
+    core.run(n, 0, n)
+    for getter, typestr in ((core.get_neighbor_indices, "<u4"), (core.get_neighbor_dists, "<f4"),
+                            (core.get_embedding, "<f4")):
+        v = getter()
+        cai = v.__cuda_array_interface__
+        assert cai["typestr"] == typestr and cai["data"][1] is True and cai["version"] == 3
+        assert cai["stream"] not in (0, None)
+        assert v.__dlpack_device__() == (2, torch.cuda.current_device())
+        side = torch.cuda.Stream()
+        with torch.cuda.stream(side):
+            t = torch.from_dlpack(v)
+            via_dl = t.clone()
+        side.synchronize()
+        holder = type("H", (), {})()
+        holder.__cuda_array_interface__ = dict(cai, data=(cai["data"][0], False))
+        via_cai = torch.as_tensor(holder, device="cuda")
+        assert tuple(via_dl.shape) == tuple(cai["shape"])
+        assert torch.equal(via_dl.view(torch.int32) if typestr == "<u4" else via_dl,
+                           via_cai.view(torch.int32) if typestr == "<u4" else via_cai)
+    # the DLPack tensor keeps the model alive
+    t = torch.from_dlpack(core.get_embedding())
+    del core
+    assert torch.isfinite(t[:n]).all()

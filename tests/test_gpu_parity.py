@@ -147,14 +147,16 @@ def test_fuzzy_schedule_operator(native, oracle_mod):
     assert np.array_equal(sg.cpu().numpy(), ref["sigma"]) and np.array_equal(rh.cpu().numpy(), ref["rho"])
 
 
-def test_sgd_operator_deterministic_case(native, oracle_mod):
+# A small and a large embedding (1,024 and 600,000 rows): both must equal
+# the oracle bit for bit.
+@pytest.mark.parametrize("n", [1024, 600_000])
+def test_sgd_operator_deterministic_case(native, oracle_mod, n):
     # disjoint edges and no negative samples: the parallel epoch has no races
     import ctypes as C
 
     import torch
 
     rng = np.random.default_rng(3)
-    n = 1024
     emb = rng.normal(size=(n, 2)).astype(np.float32)
     head = np.arange(0, 512, dtype=np.int32)
     tail = head + 512
@@ -168,6 +170,35 @@ def test_sgd_operator_deterministic_case(native, oracle_mod):
                                          4.0, 1.0, 1.0, 1.58, 0.9, 60, 0, 42,
                                          C.c_void_p(torch.cuda.current_stream().cuda_stream)))
     assert np.array_equal(te.cpu().numpy(), ref)
+
+
+def test_sgd_single_edge_with_negative_samples(native, oracle_mod):
+    # one edge: a single thread updates, so the run is race free even with
+    # negative samples; the repulsion's d^(2b) comes from the hardware pow on
+    # the GPU and from the series pow in the oracle (a few ulp apart), so the
+    # positions agree to a tolerance, not bit for bit
+    import ctypes as C
+
+    import torch
+
+    rng = np.random.default_rng(11)
+    n = 4096
+    emb = rng.normal(size=(n, 2)).astype(np.float32)
+    head, tail = np.array([7], np.int32), np.array([2001], np.int32)
+    eps = np.array([1.0], np.float32)
+    ref = oracle_mod.sgd(emb, head, tail, eps, rounding=4.0, alpha0=1.0, a=1.58, b=0.9, n_epochs=200,
+                         negative_sample_rate=5)
+    dev = torch.device("cuda:0")
+    te = torch.from_numpy(emb.copy()).to(dev)
+    th, tt, tp = (torch.from_numpy(a).to(dev) for a in (head, tail, eps))
+    native.check(native.load().gm_op_sgd(te.data_ptr(), n, th.data_ptr(), tt.data_ptr(), tp.data_ptr(), 1,
+                                         4.0, 1.0, 1.0, 1.58, 0.9, 200, 5, 42,
+                                         C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    got = te.cpu().numpy()
+    moved = np.flatnonzero(np.any(ref != emb, axis=1))
+    assert set(moved.tolist()) <= {7, 2001}
+    np.testing.assert_array_equal(np.delete(got, [7, 2001], axis=0), np.delete(emb, [7, 2001], axis=0))
+    np.testing.assert_allclose(got[[7, 2001]], ref[[7, 2001]], rtol=0, atol=2e-3)
 
 
 def test_errors_and_edge_cases(native):
@@ -213,6 +244,7 @@ def test_exact_distance_tile_accuracy(native):
     n, d = 1000, 100
     X, _ = gaussian_mixture(n, d, seed=5)
     s = native.Session(native.default_params(n_instances=n, n_features=d, device=0, precision=1))
+    s.keep_tiles(True)
     s.append_host(X)
     s.run(n, 0, 0)
     D = s.copy("exact_d", F32)[: n * n].reshape(n, n)
@@ -271,20 +303,27 @@ def test_overlap_mode_bitexact(native, oracle_mod, precision, upd):
     assert np.all(np.isfinite(emb))
     # the SGD is Hogwild-parallel (and uses half the SMs here, so its update
     # order differs): compare its outcome with the same build without
-    # overlap statistically.  Repeated runs of either mode at this size gave
-    # trustworthiness 0.81-0.85 with precision 0 (approximate lists) and
-    # 0.9588-0.9594 with precision 1 (exact lists).
-    r = native.Session(native.default_params(n_instances=n, n_features=d, n_neighbors=k, max_epoch=30,
-                                             device=0, precision=precision, overlap=0))
-    for c in range(n // step):
-        r.append_host(X[c * step : (c + 1) * step])
-        r.run(step, upd, 500)
-    ref = r.copy("embedding", F32).reshape(n, 2)
-    t_ov, t_ref = trustworthiness(X, emb, n_neighbors=k), trustworthiness(X, ref, n_neighbors=k)
-    tol = 0.05 if precision == 0 else 0.01
+    # overlap statistically.  Both modes build identical lists, so the spread
+    # is the SGD's alone: single runs at this size gave trustworthiness
+    # 0.81-0.85 with precision 0 (approximate lists) and 0.9588-0.9594 with
+    # precision 1 (exact lists).  Precision 0 compares the means of four runs
+    # of each mode (standard deviation of the difference ~0.008).
+    def build(overlap):
+        r = native.Session(native.default_params(n_instances=n, n_features=d, n_neighbors=k, max_epoch=30,
+                                                 device=0, precision=precision, overlap=overlap))
+        for c in range(n // step):
+            r.append_host(X[c * step : (c + 1) * step])
+            r.run(step, upd, 500)
+        e = r.copy("embedding", F32).reshape(n, 2)
+        r.close()
+        return trustworthiness(X, e, n_neighbors=k)
+
+    reps = 4 if precision == 0 else 1
+    t_ov = np.mean([trustworthiness(X, emb, n_neighbors=k)] + [build(1) for _ in range(reps - 1)])
+    t_ref = np.mean([build(0) for _ in range(reps)])
+    tol = 0.025 if precision == 0 else 0.01
     assert abs(t_ov - t_ref) < tol, (t_ov, t_ref)
     s.close()
-    r.close()
 
 
 @pytest.mark.parametrize("n,d,metric,k,step", [(8, 3, 0, 15, 3), (40, 5, 1, 10, 7), (300, 17, 0, 32, 64)])

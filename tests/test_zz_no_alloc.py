@@ -39,14 +39,14 @@ def _case(seed, n, nnz):
     return emb, head, tail, eps
 
 
-def _run(fn, emb, head, tail, eps, n_epochs, stream_ptr):
+def _run(fn, emb, head, tail, eps, n_epochs, stream_ptr, neg_rate=0):
     import torch
 
     dev = torch.device("cuda:0")
     te = torch.from_numpy(emb.copy()).to(dev)
     th, tt, tp = (torch.from_numpy(a).to(dev) for a in (head, tail, eps))
     rc = fn(te.data_ptr(), emb.shape[0], th.data_ptr(), tt.data_ptr(), tp.data_ptr(), head.shape[0],
-            4.0, 1.0, 1.0, 1.58, 0.9, n_epochs, 0, 42, stream_ptr)
+            4.0, 1.0, 1.0, 1.58, 0.9, n_epochs, neg_rate, 42, stream_ptr)
     torch.cuda.synchronize()
     return rc, te.cpu().numpy()
 
@@ -65,6 +65,66 @@ def test_noalloc_sgd_matches_allocating_operator_twice(native):
         assert rc_ref == 0 and rc_na == 0, lib.gm_last_error()
         assert not np.array_equal(got, emb)  # the epochs moved the points
         assert np.array_equal(got, want)
+
+
+def test_noalloc_sgd_single_edge_with_negative_samples(native):
+    # one edge, five negative samples per sampling: one thread updates, so
+    # both operators run the same sequence of operations and agree bit for bit
+    import torch
+
+    lib = native.load()
+    ref_fn, na_fn = _fn(lib, "gm_op_sgd"), _fn(lib, "gm_op_sgd_noalloc")
+    stream = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(21)
+    emb = rng.normal(size=(2048, 2)).astype(np.float32)
+    head, tail, eps = np.array([3], np.int32), np.array([1500], np.int32), np.array([1.0], np.float32)
+    for _ in range(2):
+        rc_ref, want = _run(ref_fn, emb, head, tail, eps, 200, stream, neg_rate=5)
+        rc_na, got = _run(na_fn, emb, head, tail, eps, 200, stream, neg_rate=5)
+        assert rc_ref == 0 and rc_na == 0, lib.gm_last_error()
+        assert not np.array_equal(got, emb)
+        assert np.array_equal(got, want)
+
+
+def test_noalloc_sgd_with_races_agrees_statistically(native):
+    # the 8-NN graph of a 6-cluster mixture (every row is the head of 8 edges
+    # and the tail of others, so edges share rows) with negative samples:
+    # Hogwild updates race, and the two operators visit the edges in
+    # different orders (gm_op_sgd groups them by sampling period), so the
+    # check is statistical: from a random start both reach the same
+    # trustworthiness within 0.02, on two calls in a row.  (The sequential
+    # oracle reaches 0.955 on this case.)
+    import torch
+
+    from gpumap_gb300.datasets import gaussian_mixture
+    from oracle.knn import trustworthiness
+
+    lib = native.load()
+    ref_fn, na_fn = _fn(lib, "gm_op_sgd"), _fn(lib, "gm_op_sgd_noalloc")
+    stream = torch.cuda.current_stream().cuda_stream
+    n, deg = 3000, 8
+    X, _ = gaussian_mixture(n, 8, n_centers=6, seed=31)
+    x = X.astype(np.float64)
+    sq = (x * x).sum(1)
+    d = sq[:, None] + sq[None, :] - 2.0 * (x @ x.T)
+    np.fill_diagonal(d, np.inf)
+    nbr = np.argsort(d, axis=1)[:, :deg]
+    head = np.repeat(np.arange(n, dtype=np.int32), deg)
+    tail = nbr.reshape(-1).astype(np.int32)
+    rng = np.random.default_rng(31)
+    eps = rng.uniform(1.0, 4.0, size=head.shape[0]).astype(np.float32)
+    emb = rng.normal(size=(n, 2)).astype(np.float32)
+    sample = np.arange(0, n, 3)
+    start = trustworthiness(X, emb, deg, sample=sample)
+    for _ in range(2):
+        rc_ref, want = _run(ref_fn, emb, head, tail, eps, 100, stream, neg_rate=5)
+        rc_na, got = _run(na_fn, emb, head, tail, eps, 100, stream, neg_rate=5)
+        assert rc_ref == 0 and rc_na == 0, lib.gm_last_error()
+        assert np.all(np.isfinite(got))
+        t_ref = trustworthiness(X, want, deg, sample=sample)
+        t_na = trustworthiness(X, got, deg, sample=sample)
+        assert t_ref > start + 0.3 and t_na > start + 0.3, (start, t_ref, t_na)
+        assert abs(t_ref - t_na) <= 0.02, (t_ref, t_na)
 
 
 def test_noalloc_sgd_rejects_oversized_edge_list(native):

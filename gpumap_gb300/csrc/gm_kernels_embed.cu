@@ -396,66 +396,35 @@ GM_D int sgd_n_neg(float fe, float nn, float ep_neg) {
   return (int)__fdiv_rn(__fsub_rn(fe, nn), ep_neg);
 }
 
-// Embedding positions in global memory (read through L2; a row update is one
-// float2 vector reduction, each element added atomically).
-struct GlobalPos {
-  float *emb;
-  GM_D float2 load(int r) const { return ld_pos(emb + (size_t)r * 2); }
-  GM_D void add(int r, float x, float y) const {
-    atomicAdd(reinterpret_cast<float2 *>(emb + (size_t)r * 2), make_float2(x, y));
-  }
-};
-
-// The first 8 Philox words of an edge's negative-sample stream at one epoch
-// (blocks 0 and 1; block 1 only when more than 4 samples are drawn).
-GM_D void neg_draws(int row, int n_neg, uint64_t seed, uint32_t (&w)[8]) {
-  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-  philox_block((uint32_t)row, 0u, kTagNegSample, 0u, k0, k1, w);
-  if (n_neg > 4) philox_block((uint32_t)row, 1u, kTagNegSample, 0u, k0, k1, w + 4);
-}
-
-// One edge of one epoch (reference optimize_batch_kernel,
-// embedding_kernel.cuh:509-589): the attraction moves the head and, by a
-// rounded atomic, the tail; then the negative samples repel the head.  The
-// positions of the head, the tail and of the first kNegAhead samples (rows
-// from this edge's Philox stream, words in order; ``pre`` holds them when the
-// caller drew them in advance) are fetched together, ahead of the arithmetic.
-//
-// Pinned deviation (order of the head's updates inside one edge): the
-// reference moves the head after each negative sample before the next one's
-// distance; here every repulsion is taken from the head position after the
-// attraction step and the repulsions are added in draw order.  The samples
-// of an edge are then independent, so their arithmetic runs in parallel
-// instead of as one dependent chain.  Edges update each other's rows
-// concurrently (Hogwild) in both, so the embedding is compared statistically.
-//
-// A sample that is this edge's own tail sees this thread's tail update,
-// which in sequential order precedes the read.  powf(d2, b - 1) and
-// powf(d2, b) share one log.
-GM_D void sgd_edge(const GlobalPos &pos, int row, int j, int kk, float ep, float &ns, float &nn,
-                   int n, uint64_t M, float rounding, float alpha, float fe, float gamma, float a,
-                   float b, float nsr_inv, uint64_t seed, const uint32_t *pre, unsigned &my_edges,
-                   unsigned &my_negs) {
+// One edge of one epoch.  The positions of the head, the tail and of the
+// first kNegAhead negative samples (rows from this edge's Philox stream,
+// blocks 0 and 1, words in order, computed directly into registers) are
+// fetched together, ahead of the sequential updates.  A sample that is this
+// edge's own tail is advanced by this thread's tail update, which in
+// sequential order precedes the read.  powf(d2, b - 1) and powf(d2, b) share
+// one log.
+GM_D void sgd_edge(float *emb, int row, int j, int kk, float ep, float &ns, float &nn, int n,
+                   uint64_t M, float rounding, float alpha, float fe, float gamma, float a,
+                   float b, float nsr_inv, uint64_t seed, unsigned &my_edges, unsigned &my_negs) {
   ++my_edges;
-  const float2 cpv = pos.load(j), opv = pos.load(kk);
+  float *cp = emb + (size_t)j * 2;
+  float *op = emb + (size_t)kk * 2;
+  const float2 cpv = ld_pos(cp), opv = ld_pos(op);
   float cur0 = cpv.x, cur1 = cpv.y;
   const float ep_neg = __fmul_rn(ep, nsr_inv);
   const int n_neg = sgd_n_neg(fe, nn, ep_neg);
   int rr[kNegAhead];
   float2 qq[kNegAhead];
   if (n_neg > 0) {
+    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
     uint32_t w[8];
-    if (pre) {
-#pragma unroll
-      for (int p = 0; p < 8; ++p) w[p] = pre[p];
-    } else {
-      neg_draws(row, n_neg, seed, w);
-    }
+    philox_block((uint32_t)row, 0u, kTagNegSample, 0u, k0, k1, w);
+    if (n_neg > 4) philox_block((uint32_t)row, 1u, kTagNegSample, 0u, k0, k1, w + 4);
 #pragma unroll
     for (int p = 0; p < kNegAhead; ++p) {
       if (p < n_neg) {
         rr[p] = (int)fastmod(w[p], M, (uint32_t)n);
-        qq[p] = pos.load(rr[p]);
+        qq[p] = ld_pos(emb + (size_t)rr[p] * 2);
       }
     }
   }
@@ -475,40 +444,38 @@ GM_D void sgd_edge(const GlobalPos &pos, int row, int j, int kk, float ep, float
   cur0 = __fadd_rn(cur0, g0);
   cur1 = __fadd_rn(cur1, g1);
   const float t0 = trunc_grad(rounding, -g0), t1 = trunc_grad(rounding, -g1);
-  pos.add(kk, t0, t1);
+  // both coordinates in one vector reduction (each element added
+  // atomically, exactly as two scalar adds; rows are 8-byte aligned)
+  atomicAdd(reinterpret_cast<float2 *>(op), make_float2(t0, t1));
   ns = __fadd_rn(ns, ep);
   if (n_neg > 0) {
     const float two_gb = __fmul_rn(__fmul_rn(2.0f, gamma), b);
     const float a4 = __fmul_rn(4.0f, alpha);
-    // repulsion of the head (at cur0, cur1) from a sample at q: d2n^b by the
-    // hardware exp2 / log2 (__powf); these sampled Hogwild updates are compared
-    // statistically, and the attraction above keeps the series pow
-    auto repel = [&](float q0, float q1, float &h0, float &h1) {
+    // one negative sample: repulsion from q, head moved in sequence
+    auto negative = [&](int r, float q0, float q1) {
+      if (r == j) return;
       const float ex = __fsub_rn(cur0, q0), ey = __fsub_rn(cur1, q1);
       const float d2n = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
       float rep = 0.0f;
+      // repulsion: d2n^b by the hardware exp2 / log2 (__powf); these sampled
+      // Hogwild updates are compared statistically, and the attraction
+      // above keeps the series pow
       if (d2n > 0.0f)
         rep = __fdiv_rn(two_gb, __fmul_rn(__fadd_rn(0.001f, d2n),
                                           __fadd_rn(__fmul_rn(a, __powf(d2n, b)), 1.0f)));
-      h0 = (rep > 0.0f) ? __fmul_rn(fclip(__fmul_rn(rep, ex)), alpha) : a4;
-      h1 = (rep > 0.0f) ? __fmul_rn(fclip(__fmul_rn(rep, ey)), alpha) : a4;
+      const float h0 = (rep > 0.0f) ? __fmul_rn(fclip(__fmul_rn(rep, ex)), alpha) : a4;
+      const float h1 = (rep > 0.0f) ? __fmul_rn(fclip(__fmul_rn(rep, ey)), alpha) : a4;
+      cur0 = __fadd_rn(cur0, h0);
+      cur1 = __fadd_rn(cur1, h1);
+      g0 = __fadd_rn(g0, h0);
+      g1 = __fadd_rn(g1, h1);
     };
-    float h0[kNegAhead], h1[kNegAhead];
 #pragma unroll
     for (int p = 0; p < kNegAhead; ++p) {
-      h0[p] = 0.0f;
-      h1[p] = 0.0f;
-      if (p < n_neg && rr[p] != j) {
+      if (p < n_neg) {
         const bool own = rr[p] == kk;
-        repel(own ? __fadd_rn(qq[p].x, t0) : qq[p].x, own ? __fadd_rn(qq[p].y, t1) : qq[p].y, h0[p],
-              h1[p]);
-      }
-    }
-#pragma unroll
-    for (int p = 0; p < kNegAhead; ++p) {
-      if (p < n_neg && rr[p] != j) {
-        g0 = __fadd_rn(g0, h0[p]);
-        g1 = __fadd_rn(g1, h1[p]);
+        negative(rr[p], own ? __fadd_rn(qq[p].x, t0) : qq[p].x,
+                 own ? __fadd_rn(qq[p].y, t1) : qq[p].y);
       }
     }
     if (n_neg > kNegAhead) {
@@ -518,19 +485,15 @@ GM_D void sgd_edge(const GlobalPos &pos, int row, int j, int kk, float ep, float
       g.block = kNegAhead / 4;
       for (int p = kNegAhead; p < n_neg; ++p) {
         const int r = (int)fastmod(philox_next(g), M, (uint32_t)n);
-        if (r == j) continue;
-        const float2 q = pos.load(r);
-        const bool own = r == kk;
-        float e0, e1;
-        repel(own ? __fadd_rn(q.x, t0) : q.x, own ? __fadd_rn(q.y, t1) : q.y, e0, e1);
-        g0 = __fadd_rn(g0, e0);
-        g1 = __fadd_rn(g1, e1);
+        const float2 q = ld_pos(emb + (size_t)r * 2);
+        negative(r, q.x, q.y);
       }
     }
     nn = __fadd_rn(nn, __fmul_rn((float)n_neg, ep_neg));
     my_negs += (unsigned)n_neg;
   }
-  pos.add(j, trunc_grad(rounding, g0), trunc_grad(rounding, g1));
+  atomicAdd(reinterpret_cast<float2 *>(cp),
+            make_float2(trunc_grad(rounding, g0), trunc_grad(rounding, g1)));
 }
 
 // Edges [first, nnz) step stride of one epoch, state in global memory.
@@ -544,8 +507,8 @@ GM_D void sgd_epoch_edges(float *emb, const int *head, const int *tail, const fl
     float ns = next_s[row];
     if (ns > fe) continue;
     float nn = next_n[row];
-    sgd_edge(GlobalPos{emb}, row, head[row], tail[row], eps[row], ns, nn, n, M, rounding, alpha, fe,
-             gamma, a, b, nsr_inv, seed, nullptr, my_edges, my_negs);
+    sgd_edge(emb, row, head[row], tail[row], eps[row], ns, nn, n, M, rounding, alpha, fe, gamma, a,
+             b, nsr_inv, seed, my_edges, my_negs);
     next_s[row] = ns;
     next_n[row] = nn;
   }
@@ -647,22 +610,6 @@ __global__ void __launch_bounds__(kSgdThreads)
       rns[t] = next_s[row], rnn[t] = next_n[row];
     }
   }
-  // Philox words of a register edge's next sampling, drawn while the grid
-  // waits at the epoch barrier (they depend on the edge and the epoch only)
-  uint32_t pw[kRegEdges][8];
-  bool have[kRegEdges];
-  const float nsr = nsr_inv;
-#pragma unroll
-  for (int t = 0; t < kRegEdges; ++t) {
-    have[t] = false;
-    if (first + t * stride < nnz && rns[t] <= 0.0f) {
-      const int nneg = sgd_n_neg(0.0f, rnn[t], __fmul_rn(rep[t], nsr));
-      if (nneg > 0) {
-        neg_draws(rrow[t], nneg, seed, pw[t]);
-        have[t] = true;
-      }
-    }
-  }
   float alpha = alpha0;
   for (int ep = 0; ep < n_epochs; ++ep) {
     const float fe = (float)ep;
@@ -670,34 +617,22 @@ __global__ void __launch_bounds__(kSgdThreads)
 #pragma unroll
     for (int t = 0; t < kRegEdges; ++t) {
       if (first + t * stride < nnz && rns[t] <= fe)
-        sgd_edge(GlobalPos{emb}, rrow[t], rj[t], rk[t], rep[t], rns[t], rnn[t], n, M, rounding,
-                 alpha, fe, gamma, a, b, nsr_inv, sd, have[t] ? pw[t] : nullptr, my_edges, my_negs);
+        sgd_edge(emb, rrow[t], rj[t], rk[t], rep[t], rns[t], rnn[t], n, M, rounding, alpha, fe,
+                 gamma, a, b, nsr_inv, sd, my_edges, my_negs);
     }
     for (int slot = first + kRegEdges * stride; slot < nnz; slot += stride) {
       const int row = perm ? perm[slot] : slot;
       float ns = next_s[row];
       if (ns > fe) continue;
       float nn = next_n[row];
-      sgd_edge(GlobalPos{emb}, row, head[row], tail[row], eps[row], ns, nn, n, M, rounding, alpha,
-               fe, gamma, a, b, nsr_inv, sd, nullptr, my_edges, my_negs);
+      sgd_edge(emb, row, head[row], tail[row], eps[row], ns, nn, n, M, rounding, alpha, fe, gamma,
+               a, b, nsr_inv, sd, my_edges, my_negs);
       next_s[row] = ns;
       next_n[row] = nn;
     }
     alpha = __fmul_rn(alpha0, __fsub_rn(1.0f, __fdiv_rn((float)ep, (float)n_epochs)));
     if (ep + 1 < n_epochs) {
       grid_arrive(bar);
-      const float fn = (float)(ep + 1);
-#pragma unroll
-      for (int t = 0; t < kRegEdges; ++t) {
-        have[t] = false;
-        if (first + t * stride < nnz && rns[t] <= fn) {
-          const int nneg = sgd_n_neg(fn, rnn[t], __fmul_rn(rep[t], nsr));
-          if (nneg > 0) {
-            neg_draws(rrow[t], nneg, seed + (uint64_t)(ep + 1), pw[t]);
-            have[t] = true;
-          }
-        }
-      }
       if (!grid_wait(bar, (unsigned)(ep + 1) * gridDim.x, err)) break;
     }
   }

@@ -867,10 +867,6 @@ void sgd(float *emb, int n, const int *head, const int *tail, const float *eps, 
       const float ratio = (fe - nv) / en;
       const int n_neg = (ratio > 0.0f && ratio < 2147483520.0f) ? (int)ratio : 0;
       if (n_neg > 0) {
-        // pinned deviation from the reference (embedding_kernel.cuh:555-583,
-        // which moves the head after each sample): every repulsion is taken
-        // from the head position after the attraction step, and the
-        // repulsions are added in draw order
         Rng g;
         rng_init(g, sd, (uint32_t)row, TAG_NEG);
         for (int p = 0; p < n_neg; ++p) {
@@ -883,6 +879,8 @@ void sgd(float *emb, int n, const int *head, const int *tail, const float *eps, 
           if (d2n > 0.0f) rep = ((2.0f * gamma) * b) / ((0.001f + d2n) * (a * o_powf(d2n, b) + 1.0f));
           const float h0 = rep > 0.0f ? fclip(rep * ex) * alpha : 4.0f * alpha;
           const float h1 = rep > 0.0f ? fclip(rep * ey) * alpha : 4.0f * alpha;
+          c0 = c0 + h0;
+          c1 = c1 + h1;
           g0 = g0 + h0;
           g1 = g1 + h1;
         }

@@ -163,6 +163,7 @@ Session::Session(const gm_params &p) : p_(p) {
       xs_.pool_j2 = (int *)dalloc((size_t)xs_.pool_cap * sizeof(int));
       xs_.pool_m2 = (int *)dalloc((size_t)xs_.pool_cap * sizeof(int));
       xs_.row_t = (float *)dalloc((size_t)ex_block_ * sizeof(float));
+      xs_.seed = (float *)dalloc((size_t)ex_block_ * sizeof(float));
       xs_.heaps = (float *)dalloc((size_t)ex_block_ * std::max(sms_, 1) * 32 * sizeof(float));
       xs_.pcnt = (int *)dalloc((Nm + 1) * sizeof(int));
       xs_.poff = (int *)dalloc((Nm + 1) * sizeof(int));

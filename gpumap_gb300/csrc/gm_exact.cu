@@ -199,7 +199,10 @@ GM_D float heap_push(float *h, int &cnt, float x) {
 
 // Screen state of one block of batch rows (batch-local row m).
 struct TileScreen {
+  int tile_count;     // column tiles this pass visits: tile t is column tile t * tile_stride
+  int tile_stride;
   float *heaps;       // (m * gridDim.x + CTA) * 32: each CTA's 32 smallest upper bounds of row m
+  const float *seed;  // pass 1: per-row upper bounds from pass 0 (or null)
   const float *row_t; // exact per-row thresholds (pass 2)
   int *cand;          // m * cand_ld + i: candidate columns of row m (pass 2)
   long cand_ld;
@@ -216,12 +219,17 @@ struct TileScreen {
 // leave the tensor memory (the tile itself is not stored).  grid.y: 128-row
 // tiles of the batch; grid.x: CTAs sharing the column tiles.  For every pair
 // (batch row m, column j) the epilogue forms D and the bound B (pair_bound).
-//  Pass 1 (kPass == 1): every CTA keeps, per row, a max-heap of the 32
-//    smallest upper bounds D + B it sees and stores it to sc.heaps at the
-//    end; the row's 32nd smallest upper bound over all columns is the 32nd
-//    smallest of the union of those heaps (k_row_threshold).  Column side,
-//    for an existing row j: (j, m) is stored when D - B is at most the 32nd
-//    distance of j's list.
+//  Pass 0 (kPass == 0), on 16 evenly spaced column tiles only: every CTA
+//    keeps, per row, a max-heap of the 32 smallest upper bounds D + B it
+//    sees and stores it to sc.heaps; the 32nd smallest of their union
+//    (k_row_threshold) bounds the row's 32nd smallest upper bound over all
+//    columns from above (the seed).
+//  Pass 1 (kPass == 1), all column tiles: the same heaps, fed only with
+//    upper bounds at or below the seed (a lane then rarely takes the push
+//    path, which the other lanes of its warp would wait for); the union of
+//    the heaps gives the row's exact 32nd smallest upper bound, or the seed
+//    when it holds fewer than 32.  Column side, for an existing row j:
+//    (j, m) is stored when D - B is at most the 32nd distance of j's list.
 //  Pass 2 (kPass == 2): the same tile again; j becomes a candidate of row m
 //    when D - B is at most m's exact threshold.  The candidates hold every
 //    column whose canonical distance can be among m's 32 smallest.
@@ -245,7 +253,6 @@ __global__ void __launch_bounds__(kExactThreads, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int mt = blockIdx.y;
   const int m0 = mt * kTM;  // batch-local first row of this tile
-  const int n_tiles = (n + kTN - 1) / kTN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -273,7 +280,8 @@ __global__ void __launch_bounds__(kExactThreads, 1)
   if (warp == 0) {
     if (lane == 0) {
       uint32_t it = 0;
-      for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x) {
+      for (int t = blockIdx.x; t < sc.tile_count && ok; t += gridDim.x) {
+        const int ct = t * sc.tile_stride;
         // 3 * kchunks K steps: hi.hi, hi.lo, lo.hi (x offsets are multiples of 64)
         for (int kc = 0; kc < 3 * kchunks; ++kc, ++it) {
           const uint32_t s = it % kStages, use = it / kStages;
@@ -285,7 +293,7 @@ __global__ void __launch_bounds__(kExactThreads, 1)
           unsigned char *a = base + (size_t)s * kStageBytes;
           mbar_expect_tx(&full[s], kStageBytes);
           tma_load_2d(&tm_a, &full[s], a, (seg == 2 ? dh : 0) + kx, arow0 + m0);
-          tma_load_2d(&tm_b, &full[s], a + kABytes, (seg == 1 ? dh : 0) + kx, t * kTN);
+          tma_load_2d(&tm_b, &full[s], a + kABytes, (seg == 1 ? dh : 0) + kx, ct * kTN);
         }
       }
       if (!ok) atomicOr(err, kDevErrSpin);
@@ -295,7 +303,7 @@ __global__ void __launch_bounds__(kExactThreads, 1)
       // tile tc accumulates in TMEM columns [256 (tc & 1), +256): the MMAs of
       // the next tile run while the epilogue drains this one
       uint32_t it = 0, tc = 0;
-      for (int t = blockIdx.x; t < n_tiles && ok; t += gridDim.x, ++tc) {
+      for (int t = blockIdx.x; t < sc.tile_count && ok; t += gridDim.x, ++tc) {
         const uint32_t b = tc & 1u, use = tc >> 1;
         if (use > 0 && !mbar_wait(&tmem_empty[b], (use - 1) & 1)) {
           ok = false;
@@ -339,11 +347,12 @@ __global__ void __launch_bounds__(kExactThreads, 1)
     float *stg = epi + (size_t)quarter * 32 * kStagePitch;
     float *heap = heaps + r;
     int hcnt = 0;
-    float t_loc = inf;  // pass 1: the heap's largest once it holds 32
+    float t_loc = inf;  // passes 0 and 1: the heap's largest once it holds 32
     const float t_row = (kPass == 2 && live) ? sc.row_t[m] : inf;
+    const float seed = (kPass == 1 && live && sc.seed) ? sc.seed[m] : inf;
     int *cand_m = sc.cand + (long)m * sc.cand_ld;
     uint32_t tc = 0;
-    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++tc) {
+    for (int t = blockIdx.x; t < sc.tile_count; t += gridDim.x, ++tc) {
       const uint32_t b = tc & 1u;
       if (!mbar_wait(&tmem_full[b], (tc >> 1) & 1)) {
         if (lane == 0) atomicOr(err, kDevErrSpin);
@@ -353,7 +362,7 @@ __global__ void __launch_bounds__(kExactThreads, 1)
       for (int c = 0; c < kTN; c += 32) {
         uint32_t v[32];
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + b * (uint32_t)kTN + (uint32_t)c, v);
-        const int col0 = t * kTN + c;
+        const int col0 = t * sc.tile_stride * kTN + c;
         const int jl = col0 + lane;
         const float njl = jl < n ? norms[jl] : 0.0f;
         const float sjl = jl < n ? snorms[jl] : 0.0f;
@@ -367,12 +376,14 @@ __global__ void __launch_bounds__(kExactThreads, 1)
           const float dv = __fsub_rn(__fadd_rn(nm, nj), __fmul_rn(2.0f, __uint_as_float(v[i])));
           if (kKeepD) stg[lane * kStagePitch + i] = dv;
           const float bnd = pair_bound(sc.coef, sm, sj, nm, nj);
-          if (kPass == 1) {
-            const float wj = __shfl_sync(0xffffffffu, wjl, i);
+          if (kPass <= 1) {
             if (live && j < n && j != row) {
               const float ub = fmaxf(__fadd_ru(dv, bnd), 0.0f);
-              if (ub < t_loc) t_loc = heap_push(heap, hcnt, ub);
+              if (ub < t_loc && ub <= seed) t_loc = heap_push(heap, hcnt, ub);
             }
+          }
+          if (kPass == 1) {
+            const float wj = __shfl_sync(0xffffffffu, wjl, i);
             const bool hit = live && j < sc.n_exist && __fsub_rd(dv, bnd) <= wj;
             const unsigned bal = __ballot_sync(0xffffffffu, hit);
             if (bal) {
@@ -390,7 +401,7 @@ __global__ void __launch_bounds__(kExactThreads, 1)
                 }
               }
             }
-          } else if (live && j < n && j != row && __fsub_rd(dv, bnd) <= t_row) {
+          } else if (kPass == 2 && live && j < n && j != row && __fsub_rd(dv, bnd) <= t_row) {
             cand_m[atomicAdd(&sc.row_cnt[m], 1)] = j;
           }
         }
@@ -409,7 +420,7 @@ __global__ void __launch_bounds__(kExactThreads, 1)
       tc_fence_before();
       mbar_arrive(&tmem_empty[b]);
     }
-    if (kPass == 1 && live) {
+    if (kPass <= 1 && live) {
       float *out = sc.heaps + ((size_t)m * gridDim.x + blockIdx.x) * kListTop;
       for (int i = 0; i < kListTop; ++i) out[i] = i < hcnt ? heap[i * kTM] : inf;
     }
@@ -449,7 +460,7 @@ constexpr int kTileLd = 33;
 constexpr int kFinalWarps = 4;
 
 __global__ void __launch_bounds__(kFinalWarps * 32)
-    k_row_threshold(const float *heaps, int ncta, int nrows, int n, float *row_t,
+    k_row_threshold(const float *heaps, int ncta, int nrows, int n, const float *seed, float *row_t,
                     unsigned long long *stat) {
   const int lane = threadIdx.x & 31;
   const int ml = blockIdx.x * kFinalWarps + (threadIdx.x >> 5);
@@ -474,7 +485,9 @@ __global__ void __launch_bounds__(kFinalWarps * 32)
       else if (lane == pos) top = x;
     }
   }
-  const float T = __shfl_sync(0xffffffffu, top, 31);
+  // the 32nd smallest of the union (inf when it holds fewer than 32), capped
+  // by the seed: both bound the row's 32nd smallest upper bound from above
+  const float T = fminf(__shfl_sync(0xffffffffu, top, 31), seed ? seed[ml] : inf);
   if (lane == 0) {
     // fewer than 32 other rows: every column is a candidate
     row_t[ml] = n - 1 < kListTop ? inf : T;
@@ -763,7 +776,7 @@ void launch_to_bf16(const DevState &st, void *xh, int dh, int row0, int nrows, c
 template <int kPass, bool kKeepD>
 static void launch_tile(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
                         int nrows, int n, const ExactScreen &x, long ldD, int gx, int m_tiles,
-                        cudaStream_t s) {
+                        int tile_count, int tile_stride, const float *seed, cudaStream_t s) {
   // once per device (sessions on several host threads may launch at once)
   static std::atomic<unsigned> configured{0u};
   int dev = 0;
@@ -777,7 +790,10 @@ static void launch_tile(const DevState &st, const ExactMaps &maps, int dh, int r
   memcpy(&ta, maps.a, sizeof(ta));
   memcpy(&tb, maps.b, sizeof(tb));
   TileScreen sc;
+  sc.tile_count = tile_count;
+  sc.tile_stride = tile_stride;
   sc.heaps = x.heaps;
+  sc.seed = seed;
   sc.row_t = x.row_t;
   sc.cand = x.cand;
   sc.cand_ld = ldD;
@@ -794,6 +810,9 @@ static void launch_tile(const DevState &st, const ExactMaps &maps, int dh, int r
   note_launch();
 }
 
+// Column tiles of the seed pass (evenly spaced over the columns).
+constexpr int kSeedTiles = 16;
+
 void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
                        int nrows, int n, const ExactScreen &x, long ldD, bool keep_d, int sms,
                        cudaStream_t s) {
@@ -803,14 +822,26 @@ void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int ro
   const int gx = std::max(1, std::min(n_tiles, std::max(1, sms / m_tiles)));
   cudaMemsetAsync(x.row_cnt, 0, (size_t)nrows * sizeof(int), s);
   cudaMemsetAsync(x.counter, 0, sizeof(int), s);
+  const float *seed = nullptr;
+  if (n_tiles > 2 * kSeedTiles) {
+    // seed pass: the 32nd smallest upper bound over 16 spread tiles
+    const int stride = n_tiles / kSeedTiles;
+    const int gx0 = std::max(1, std::min(kSeedTiles, std::max(1, sms / m_tiles)));
+    launch_tile<0, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx0, m_tiles, kSeedTiles, stride,
+                          nullptr, s);
+    k_row_threshold<<<cdiv(nrows, kFinalWarps), kFinalWarps * 32, 0, s>>>(x.heaps, gx0, nrows, n, nullptr,
+                                                                          x.seed, nullptr);
+    note_launch();
+    seed = x.seed;
+  }
   if (keep_d && x.D)
-    launch_tile<1, true>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, s);
+    launch_tile<1, true>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, seed, s);
   else
-    launch_tile<1, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, s);
-  k_row_threshold<<<cdiv(nrows, kFinalWarps), kFinalWarps * 32, 0, s>>>(x.heaps, gx, nrows, n, x.row_t,
-                                                                        st.stat);
+    launch_tile<1, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, seed, s);
+  k_row_threshold<<<cdiv(nrows, kFinalWarps), kFinalWarps * 32, 0, s>>>(x.heaps, gx, nrows, n, seed,
+                                                                        x.row_t, st.stat);
   note_launch();
-  launch_tile<2, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, s);
+  launch_tile<2, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, nullptr, s);
 }
 
 void launch_exact_screen(const DevState &st, int row0, int blk0, int nrows, int n,

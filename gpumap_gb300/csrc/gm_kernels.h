@@ -112,6 +112,7 @@ struct ExactScreen {
   int *row_cnt = nullptr;     // rows candidate counts
   float *heaps = nullptr;     // rows x CTAs x 32: per-CTA smallest upper bounds (pass 1)
   float *row_t = nullptr;     // rows exact thresholds
+  float *seed = nullptr;      // rows thresholds from the seed pass
   int *pool_j = nullptr, *pool_m = nullptr;    // column pairs as found
   int *pool_j2 = nullptr, *pool_m2 = nullptr;  // grouped by existing row
   float *pool_d = nullptr;    // their canonical distances

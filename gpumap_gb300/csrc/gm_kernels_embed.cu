@@ -595,9 +595,14 @@ __global__ void __launch_bounds__(kSgdThreads)
   const uint64_t M = ~0ull / (uint64_t)max(n, 1) + 1ull;
   const float rounding = fscal[FS_ROUND];
   unsigned my_edges = 0, my_negs = 0;
-  const int first = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
   // slot i of the grid handles edge perm[i] (edges grouped by sampling period,
-  // so that a warp's lanes tend to be active in the same epochs)
+  // so that a warp's lanes tend to be active in the same epochs).  Warp-sized
+  // runs of slots are dealt round-robin over the CTAs (run w to CTA
+  // w mod gridDim.x), so the edges of each period, and the busiest ones,
+  // spread over every SM instead of filling the first few; the map from
+  // (CTA, thread) to slot is a bijection on [0, gridDim.x * blockDim.x).
+  const int first = (((int)threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x) * 32 + ((int)threadIdx.x & 31);
+  const int stride = gridDim.x * blockDim.x;
   int rrow[kRegEdges], rj[kRegEdges], rk[kRegEdges];
   float rep[kRegEdges], rns[kRegEdges], rnn[kRegEdges];
 #pragma unroll

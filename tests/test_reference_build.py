@@ -7,10 +7,12 @@ two of its runs already differ; the comparisons are of what both must share:
 
 * the stored distance of every listed pair is the metric's distance of that
   pair (squared L2; 2 (1 - cos) for cosine) in both builds, to FP32 rounding;
-* recall@k of the plain path (precision 0, the reference's algorithm) agrees
-  with the reference's on the same schedule within 0.05, and the precision
-  form's lists are exact;
-* trustworthiness of the two embeddings agrees within 0.03.
+* every published slot of this build is filled after insertion; the
+  reference leaves some rows' slots unfilled (id UINT_MAX, dist FLT_MAX) on
+  this schedule, so the quality comparisons are one-sided: recall@k of the
+  plain path (precision 0, the reference's algorithm) is at least the
+  reference's minus 0.05, trustworthiness at least the reference's minus
+  0.03, and the precision form's lists are exact.
 
 Skipped when the reference build is absent.
 """
@@ -88,9 +90,11 @@ def test_plain_path_agrees_with_reference_build(native, metric, n, d, seed):
     o_ids, o_dist, o_emb = _ours(native, X, k, metric, 0, chunk, upd, emb)
 
     # stored distance convention, pinned to the reference's own output
-    for ids, dist in ((r_ids, r_dist), (o_ids, o_dist)):
-        ok = (ids >= 0) & (ids < n) & (dist < 1e30)
-        assert ok.mean() > 0.99
+    r_ok = (r_ids >= 0) & (r_ids < n) & (r_dist < 1e30)
+    o_ok = (o_ids >= 0) & (o_ids < n) & (o_dist < 1e30)
+    assert o_ok.all(), np.flatnonzero(~o_ok.all(1))[:10]
+    assert r_ok.mean() > 0.5, r_ok.mean()
+    for ids, dist, ok in ((r_ids, r_dist, r_ok), (o_ids, o_dist, o_ok)):
         want = _pair_dists(X, np.where(ok, ids, 0), metric)
         err = np.abs(dist.astype(np.float64) - want)[ok]
         assert np.all(err <= 1e-4 * np.abs(want[ok]) + 1e-4), err.max()
@@ -99,12 +103,12 @@ def test_plain_path_agrees_with_reference_build(native, metric, n, d, seed):
     ex, _ = exact_knn(X, k, queries=q, metric=metric)
     rec_r = recall_at_k(r_ids[q], ex)
     rec_o = recall_at_k(o_ids[q], ex)
-    assert abs(rec_o - rec_r) <= 0.05, (rec_o, rec_r)
+    assert rec_o >= rec_r - 0.05, (rec_o, rec_r, 1.0 - r_ok.mean())
 
     sample = np.arange(0, n, 6)
     t_r = trustworthiness(X, r_emb, k, sample=sample)
     t_o = trustworthiness(X, o_emb, k, sample=sample)
-    assert abs(t_o - t_r) <= 0.03, (t_o, t_r)
+    assert t_o >= t_r - 0.03, (t_o, t_r)
 
 
 def test_precision_form_is_exact_where_reference_is_approximate(native):

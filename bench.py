@@ -81,6 +81,8 @@ def parse():
     ap.add_argument("--no-u2000", action="store_true")
     ap.add_argument("--no-run10", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--rows", type=int, default=None,
+                    help="cosine-1m only: the same generator with ROWS rows (profiling); default 1,000,000")
     ap.add_argument("--workload", default="image-70k", choices=["image-70k", "cosine-1m", "serving", "batched-64"],
                     help="image-70k: the headline line; the others print their own line")
     return ap.parse_args()
@@ -757,7 +759,8 @@ def main():
         torch.cuda.set_device(0)
         _native.load()
         if args.workload == "cosine-1m":
-            print(json.dumps({"workload_line": "cosine-1m", **cosine_1m_run(_native)}))
+            kw = {"n": args.rows, "fp32_rows": min(200_000, args.rows)} if args.rows else {}
+            print(json.dumps({"workload_line": "cosine-1m", **cosine_1m_run(_native, **kw)}))
         elif args.workload == "batched-64":
             print(json.dumps({"workload_line": "batched-64", **batched_run(_native)}))
         else:

@@ -63,6 +63,7 @@ class gm_stats(C.Structure):
         ("exact_launches", C.c_uint64), ("exact_ms", C.c_double), ("exact_flops", C.c_double),
         ("screen_ms", C.c_double), ("exact_pairs", C.c_uint64), ("exact_rescored", C.c_uint64),
         ("phase_s", C.c_double * 3),
+        ("exact_overflow_blocks", C.c_uint64),
     ]
 
 
@@ -89,6 +90,7 @@ _SIGS = [
     ("gm_debug_buffer_size", C.c_int, [_P, C.c_int, C.POINTER(C.c_uint64)]),
     ("gm_debug_copy", C.c_int, [_P, C.c_int, _P, C.c_uint64]),
     ("gm_debug_keep_tiles", C.c_int, [_P, C.c_int]),
+    ("gm_debug_pre_capacity", C.c_int, [_P, C.c_int]),
     ("gm_debug_scalars", C.c_int, [_P, C.POINTER(C.c_int64), C.c_int]),
     ("gm_debug_update_queue", C.c_int, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
     ("gm_op_fuzzy_schedule", C.c_int,
@@ -201,6 +203,9 @@ class Session:
 
     def keep_tiles(self, on: bool) -> None:
         check(self._lib.gm_debug_keep_tiles(self._h, 1 if on else 0))
+
+    def pre_capacity(self, cap: int) -> None:
+        check(self._lib.gm_debug_pre_capacity(self._h, int(cap)))
 
     def set_stats(self, on: bool) -> None:
         check(self._lib.gm_set_stats(self._h, 1 if on else 0))

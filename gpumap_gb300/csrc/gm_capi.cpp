@@ -278,6 +278,12 @@ int gm_debug_keep_tiles(gm_session *s, int on) {
   return GM_OK;
 }
 
+int gm_debug_pre_capacity(gm_session *s, int cap) {
+  if (!s) return fail(GM_ERR_INVALID, "null session");
+  if (cap < 0) return fail(GM_ERR_INVALID, "negative capacity");
+  return guarded([&] { s->impl->set_pre_cap(cap); });
+}
+
 int gm_debug_scalars(const gm_session *s, int64_t *out, int n) {
   if (!s || !out) return fail(GM_ERR_INVALID, "null argument");
   s->impl->debug_scalars(out, n);

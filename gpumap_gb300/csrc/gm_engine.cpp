@@ -164,6 +164,17 @@ Session::Session(const gm_params &p) : p_(p) {
       xs_.pool_m2 = (int *)dalloc((size_t)xs_.pool_cap * sizeof(int));
       xs_.row_t = (float *)dalloc((size_t)ex_block_ * sizeof(float));
       xs_.seed = (float *)dalloc((size_t)ex_block_ * sizeof(float));
+      // pre-candidate segments: one per (block row, CTA of a row tile), for
+      // every grid width a block can take (at most one CTA per column tile)
+      xs_.pre_cap = pre_cap_alloc_ = 64;
+      xs_.pre_gx = (int)std::min<size_t>(std::max(sms_, 1), (Nm + 255) / 256);
+      xs_.pre = (unsigned long long *)dalloc((size_t)ex_block_ * xs_.pre_gx * xs_.pre_cap *
+                                             sizeof(unsigned long long));
+      xs_.pre_ub = (float *)dalloc((size_t)ex_block_ * xs_.pre_gx * xs_.pre_cap * sizeof(float));
+      xs_.mins_ld = exact_seed_tiles((int)((Nm + 255) / 256)) * 8;
+      xs_.mins = (float *)dalloc((size_t)ex_block_ * xs_.mins_ld * sizeof(float));
+      xs_.pre_cnt = (int *)dalloc((size_t)ex_block_ * xs_.pre_gx * sizeof(int));
+      xs_.pre_over = (int *)dalloc(sizeof(int));
       xs_.heaps = (float *)dalloc((size_t)ex_block_ * std::max(sms_, 1) * 32 * sizeof(float));
       xs_.pcnt = (int *)dalloc((Nm + 1) * sizeof(int));
       xs_.poff = (int *)dalloc((Nm + 1) * sizeof(int));
@@ -318,6 +329,11 @@ void Session::ensure_cand(size_t rows) {
   cand_rows_ = r;
 }
 
+void Session::set_pre_cap(int cap) {
+  drain();
+  xs_.pre_cap = std::max(0, std::min(cap, pre_cap_alloc_));
+}
+
 void Session::set_keep_tile(bool on) {
   if (on && p_.precision == 1 && !ex_D_) {
     drain();
@@ -470,6 +486,7 @@ void Session::get_stats(gm_stats *out) {
   stats_.exact_rescored = h[6];
   stats_.sgd_edges = h[7];
   stats_.sgd_negatives = h[8];
+  stats_.exact_overflow_blocks = h[9];
   stats_.kernel_launches = launch_counter();
   *out = stats_;
 }
@@ -631,9 +648,10 @@ uint32_t Session::insert(uint32_t n_ops) {
       timed_begin(4);
       launch_exact_screen(st_, row0, b0, rows, ncol, xs_, (long)ncol, sms_, s);
       timed_end(4);
-      // three BF16 products per padded feature (hi.hi, hi.lo, lo.hi), two
-      // passes over the tile
-      const uint64_t flops = 12ull * (uint64_t)rows * (uint64_t)ncol * (uint64_t)dh_;
+      // algorithmic work: three BF16 products per padded feature (hi.hi,
+      // hi.lo, lo.hi) for every pair, once (the seed pass, and pass 2 after
+      // an overflow, are overhead on the same pairs)
+      const uint64_t flops = 6ull * (uint64_t)rows * (uint64_t)ncol * (uint64_t)dh_;
       stats_.exact_flops += (double)(stats_on_ ? flops : 0);
     }
   } else {

@@ -77,6 +77,7 @@ class Session {
   size_t growth_bytes(uint32_t n_ins, uint32_t n_emb) const;
   // keep each insertion block's approximate distance tile (tests)
   void set_keep_tile(bool on);
+  void set_pre_cap(int cap);
   void drain();
   // consumer waits (on the device) for everything queued on this session
   void order_after(cudaStream_t consumer) const;
@@ -158,6 +159,7 @@ class Session {
   // statistics
   bool stats_on_ = false;
   bool keep_tile_ = false;
+  int pre_cap_alloc_ = 0;  // pre-candidate segment length allocated (precision 1)
   gm_stats stats_{};
   struct EvPair { cudaEvent_t a, b; int slot; };
   std::vector<EvPair> ev_pending_;

@@ -39,15 +39,20 @@ namespace {
 constexpr int kTM = 128;                       // batch rows per tile (MMA M)
 constexpr int kTN = 256;                       // columns per tile (MMA N)
 constexpr int kTK = 64;                        // bf16 per K chunk = one 128-byte swizzle row
-constexpr int kStages = 4;
+// A stage holds one K chunk of all four operand halves (A hi | A lo | B hi |
+// B lo) and feeds all three products of the split (12 MMAs of K = 16), so a
+// byte in flight carries 1.5x the work of one product per stage and B's hi
+// half is fetched once instead of twice.
+constexpr int kStages = 2;
 constexpr int kABytes = kTM * kTK * 2;         // 16 KB
 constexpr int kBBytes = kTN * kTK * 2;         // 32 KB
-constexpr int kStageBytes = kABytes + kBBytes; // 48 KB
+constexpr int kStageBytes = 2 * kABytes + 2 * kBBytes; // 96 KB
 constexpr int kExactThreads = 192;             // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr int kTmemCols = 512;                 // two 128 x 256 FP32 accumulators
 constexpr uint32_t kWaitLimit = 1u << 24;      // bounded mbarrier waits
-constexpr int kStagePitch = 33;                // epilogue staging row pitch (floats)
-constexpr size_t kEpiBytes = (size_t)4 * 32 * kStagePitch * sizeof(float);
+// epilogue column buffer: the 256 columns' squared norms, bound factors and
+// list bars of a tile, double buffered (two tiles)
+constexpr size_t kEpiBytes = (size_t)2 * 3 * kTN * sizeof(float);
 constexpr int kListTop = 32;                   // list width the screen keeps exact
 constexpr size_t kHeapBytes = (size_t)kListTop * kTM * sizeof(float);
 constexpr size_t kExactSmem = (size_t)kStages * kStageBytes + 1024 + 256 + kEpiBytes + kHeapBytes;
@@ -95,6 +100,18 @@ GM_D void tma_load_2d(const CUtensorMap *map, uint64_t *bar, void *dst, int x, i
       "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
       : "memory");
 }
+// The same with an L2 cache policy (createpolicy) for the lines it reads.
+GM_D void tma_load_2d_hint(const CUtensorMap *map, uint64_t *bar, void *dst, int x, int y,
+                           uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint "
+      "[%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
+}
+// Column tiles stream through L2 once per row tile while other kernels of
+// the session (the embedding's SGD) work out of L2: their lines go first.
+constexpr bool kStreamEvictFirst = true;
 
 // Shared-memory matrix descriptor: K-major operand, 128-byte swizzle,
 // 8-row groups 1024 bytes apart (stride byte offset), descriptor version 1.
@@ -202,7 +219,9 @@ struct TileScreen {
   int tile_count;     // column tiles this pass visits: tile t is column tile t * tile_stride
   int tile_stride;
   float *heaps;       // (m * gridDim.x + CTA) * 32: each CTA's 32 smallest upper bounds of row m
-  const float *seed;  // pass 1: per-row upper bounds from pass 0 (or null)
+  const float *seed;  // passes 1 and 3: per-row upper bounds from pass 0 (or null)
+  float *mins;        // pass 0: m * mins_ld + 8 * t + c: smallest upper bound of row m over
+  int mins_ld;        //   the 32 columns of chunk c of sampled tile t
   const float *row_t; // exact per-row thresholds (pass 2)
   int *cand;          // m * cand_ld + i: candidate columns of row m (pass 2)
   long cand_ld;
@@ -213,33 +232,56 @@ struct TileScreen {
   const Key *g_key;   // working lists (the 32nd entry of an existing row is its bar)
   int n_exist;        // rows [0, n_exist) are the existing rows
   float coef;
+  // pass 3: the stored columns of row m seen by CTA c, packed (lower bound
+  // bits << 32 | column) with their upper bounds in pre_ub, in segment
+  // (m * gridDim.x + c) of pre_cap entries; pre_cnt holds each segment's
+  // length and pre_over is set when one would exceed pre_cap
+  unsigned long long *pre;
+  float *pre_ub;
+  int *pre_cnt;
+  int pre_cap;
+  int *pre_over;
+  int col_test;       // pass 1: run the column test (off when pass 3 already did)
+  const int *run_if;  // when set, the launch does nothing unless *run_if != 0
 };
 
 // Distances of a block of batch rows against all columns, screened as they
 // leave the tensor memory (the tile itself is not stored).  grid.y: 128-row
 // tiles of the batch; grid.x: CTAs sharing the column tiles.  For every pair
-// (batch row m, column j) the epilogue forms D and the bound B (pair_bound).
-//  Pass 0 (kPass == 0), on 16 evenly spaced column tiles only: every CTA
-//    keeps, per row, a max-heap of the 32 smallest upper bounds D + B it
-//    sees and stores it to sc.heaps; the 32nd smallest of their union
-//    (k_row_threshold) bounds the row's 32nd smallest upper bound over all
-//    columns from above (the seed).
-//  Pass 1 (kPass == 1), all column tiles: the same heaps, fed only with
-//    upper bounds at or below the seed (a lane then rarely takes the push
-//    path, which the other lanes of its warp would wait for); the union of
-//    the heaps gives the row's exact 32nd smallest upper bound, or the seed
-//    when it holds fewer than 32.  Column side, for an existing row j:
-//    (j, m) is stored when D - B is at most the 32nd distance of j's list.
-//  Pass 2 (kPass == 2): the same tile again; j becomes a candidate of row m
-//    when D - B is at most m's exact threshold.  The candidates hold every
-//    column whose canonical distance can be among m's 32 smallest.
-// With kKeepD (pass 1 only) the tile is also written to D (ldD columns per
-// row), for tests.
+// (batch row m, column j) the epilogue forms D and the bound B (pair_bound);
+// its upper bound is D + B and its lower bound D - B.  Past 32 column tiles:
+//  Pass 0 (kPass == 0), on an evenly spaced sample of column tiles: per row
+//    and 32-column chunk, the smallest upper bound (sc.mins).  The 32nd
+//    smallest of a row's chunk minima (k_seed_select) is the largest upper
+//    bound of 32 distinct columns, so it bounds the row's 32nd smallest
+//    upper bound over all columns from above: the seed.
+//  Pass 3 (kPass == 3), all column tiles: every column whose lower bound is
+//    at most the seed is stored with its bounds.  Every column whose upper
+//    bound is at most the row's exact threshold T (its 32nd smallest upper
+//    bound) is among them, so k_pre_select finds T exactly from the stored
+//    upper bounds, then keeps the stored columns with lower bound <= T.
+//    Column side, for an existing row j: (j, m) goes to the pair pool when
+//    D - B is at most the 32nd distance of j's list.
+// Up to 32 column tiles, and for a block whose stored columns overflowed:
+//  Pass 1 (kPass == 1), all column tiles: every CTA keeps, per row, a
+//    max-heap of the 32 smallest upper bounds it sees (at or below the seed
+//    when there is one) and stores it to sc.heaps; the 32nd smallest of
+//    their union (k_row_threshold) is T, or the seed when smaller.  The
+//    column test as in pass 3 (sc.col_test; off after a pass 3).
+//  Pass 2 (kPass == 2): the same tiles again; j becomes a candidate of row m
+//    when D - B <= T.
+// Either way the candidates hold every column whose canonical distance can
+// be among m's 32 smallest.  With kKeepD the tile is also written to D (ldD
+// columns per row), for tests.
 template <int kPass, bool kKeepD>
 __global__ void __launch_bounds__(kExactThreads, 1)
     k_exact_dist(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
                  int arow0, int nb, int n, int kchunks, int dh, const float *norms,
                  const float *snorms, TileScreen sc, float *D, long ldD, unsigned *err) {
+  // a gated launch (the fallback after a pass 3 whose stored columns did
+  // not overflow) does nothing: the flag is read before any barrier or
+  // tensor memory is set up, by every thread alike
+  if (sc.run_if && *sc.run_if == 0) return;
   extern __shared__ __align__(1024) unsigned char raw[];
   unsigned char *base = (unsigned char *)(((uintptr_t)raw + 1023) & ~(uintptr_t)1023);
   uint64_t *full = (uint64_t *)(base + (size_t)kStages * kStageBytes);
@@ -280,20 +322,30 @@ __global__ void __launch_bounds__(kExactThreads, 1)
   if (warp == 0) {
     if (lane == 0) {
       uint32_t it = 0;
+      uint64_t pol = 0;
+      if (kStreamEvictFirst) asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
       for (int t = blockIdx.x; t < sc.tile_count && ok; t += gridDim.x) {
         const int ct = t * sc.tile_stride;
-        // 3 * kchunks K steps: hi.hi, hi.lo, lo.hi (x offsets are multiples of 64)
-        for (int kc = 0; kc < 3 * kchunks; ++kc, ++it) {
+        // kchunks K chunks, each with the hi and lo halves of both operands
+        // (x offsets are multiples of 64; lo halves start at x = dh)
+        for (int kc = 0; kc < kchunks; ++kc, ++it) {
           const uint32_t s = it % kStages, use = it / kStages;
           if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1)) {
             ok = false;
             break;
           }
-          const int seg = kc / kchunks, kx = (kc - seg * kchunks) * kTK;
+          const int kx = kc * kTK;
           unsigned char *a = base + (size_t)s * kStageBytes;
           mbar_expect_tx(&full[s], kStageBytes);
-          tma_load_2d(&tm_a, &full[s], a, (seg == 2 ? dh : 0) + kx, arow0 + m0);
-          tma_load_2d(&tm_b, &full[s], a + kABytes, (seg == 1 ? dh : 0) + kx, ct * kTN);
+          tma_load_2d(&tm_a, &full[s], a, kx, arow0 + m0);
+          tma_load_2d(&tm_a, &full[s], a + kABytes, dh + kx, arow0 + m0);
+          if (kStreamEvictFirst) {
+            tma_load_2d_hint(&tm_b, &full[s], a + 2 * kABytes, kx, ct * kTN, pol);
+            tma_load_2d_hint(&tm_b, &full[s], a + 2 * kABytes + kBBytes, dh + kx, ct * kTN, pol);
+          } else {
+            tma_load_2d(&tm_b, &full[s], a + 2 * kABytes, kx, ct * kTN);
+            tma_load_2d(&tm_b, &full[s], a + 2 * kABytes + kBBytes, dh + kx, ct * kTN);
+          }
         }
       }
       if (!ok) atomicOr(err, kDevErrSpin);
@@ -311,19 +363,22 @@ __global__ void __launch_bounds__(kExactThreads, 1)
         }
         tc_fence_after();
         const uint32_t acc = tmem + b * (uint32_t)kTN;
-        for (int kc = 0; kc < 3 * kchunks; ++kc, ++it) {
+        for (int kc = 0; kc < kchunks; ++kc, ++it) {
           const uint32_t s = it % kStages, u2 = it / kStages;
           if (!mbar_wait(&full[s], u2 & 1)) {
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t a = smem_u32(base + (size_t)s * kStageBytes);
-          const uint32_t bb = a + kABytes;
+          const uint32_t ahi = smem_u32(base + (size_t)s * kStageBytes);
+          const uint32_t alo = ahi + kABytes, bhi = ahi + 2 * kABytes, blo = bhi + kBBytes;
+          // a.b = hi.hi + hi.lo + lo.hi, K = 16 at a time
 #pragma unroll
-          for (int k = 0; k < kTK / 16; ++k)
-            umma_bf16(acc, sw128_desc(a + k * 32), sw128_desc(bb + k * 32),
-                      (kc | k) != 0 ? 1u : 0u);
+          for (int k = 0; k < kTK / 16; ++k) {
+            umma_bf16(acc, sw128_desc(ahi + k * 32), sw128_desc(bhi + k * 32), (kc | k) != 0 ? 1u : 0u);
+            umma_bf16(acc, sw128_desc(ahi + k * 32), sw128_desc(blo + k * 32), 1u);
+            umma_bf16(acc, sw128_desc(alo + k * 32), sw128_desc(bhi + k * 32), 1u);
+          }
           umma_commit(&empty[s]);
         }
         if (!ok) break;
@@ -334,56 +389,95 @@ __global__ void __launch_bounds__(kExactThreads, 1)
     __syncwarp();
   } else {
     // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (tile rows), one row
-    // per thread, 32 columns per tcgen05.ld; column norms, bound factors and
-    // list bars are loaded one column per lane and passed by shuffles
+    // per thread, 32 columns per tcgen05.ld.  The four warps load a tile's
+    // column data (squared norms, bound factors, list bars) once, one tile
+    // ahead, into a double-buffered shared array that every lane reads by
+    // broadcast; each tile begins with a barrier of the 128 epilogue threads
+    // (named barrier 1), executed the same number of times by every warp.
     const int quarter = warp & 3;
     const int r = quarter * 32 + lane;
     const int m = m0 + r;
     const bool live = m < nb;
     const int row = arow0 + m;
+    const int et = threadIdx.x - 64;  // 0..127 over the epilogue warps
     const float nm = live ? norms[row] : 0.0f;
     const float sm = live ? snorms[row] : 0.0f;
     const float inf = __int_as_float(0x7f800000);
-    float *stg = epi + (size_t)quarter * 32 * kStagePitch;
     float *heap = heaps + r;
     int hcnt = 0;
     float t_loc = inf;  // passes 0 and 1: the heap's largest once it holds 32
     const float t_row = (kPass == 2 && live) ? sc.row_t[m] : inf;
-    const float seed = (kPass == 1 && live && sc.seed) ? sc.seed[m] : inf;
+    const float seed = ((kPass == 1 || kPass == 3) && live && sc.seed) ? sc.seed[m] : inf;
     int *cand_m = sc.cand + (long)m * sc.cand_ld;
+    // pass 3: this thread's segment of stored columns (row m, this CTA)
+    const size_t seg = ((size_t)m * gridDim.x + blockIdx.x) * (size_t)sc.pre_cap;
+    int pcnt = 0;
+    const bool col_test = kPass == 3 || (kPass == 1 && sc.col_test);
+    // this thread's two columns of a tile: et and et + 128
+    float cv[6];
+    auto load_cols = [&](int t) {
+      const int c0 = t * sc.tile_stride * kTN;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int j = c0 + et + h * 128;
+        cv[3 * h] = j < n ? norms[j] : 0.0f;
+        cv[3 * h + 1] = j < n ? snorms[j] : 0.0f;
+        cv[3 * h + 2] = ((kPass == 1 || kPass == 3) && j < sc.n_exist)
+                            ? key_dist(sc.g_key[(size_t)j * kListW + kListW - 1])
+                            : -inf;
+      }
+    };
+    if ((int)blockIdx.x < sc.tile_count) load_cols(blockIdx.x);
+    bool eok = true;
     uint32_t tc = 0;
     for (int t = blockIdx.x; t < sc.tile_count; t += gridDim.x, ++tc) {
       const uint32_t b = tc & 1u;
-      if (!mbar_wait(&tmem_full[b], (tc >> 1) & 1)) {
-        if (lane == 0) atomicOr(err, kDevErrSpin);
-        break;
+      float *cn = epi + (size_t)b * 3 * kTN;  // norms | bound factors | list bars
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        cn[et + h * 128] = cv[3 * h];
+        cn[kTN + et + h * 128] = cv[3 * h + 1];
+        cn[2 * kTN + et + h * 128] = cv[3 * h + 2];
       }
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+      if (t + (int)gridDim.x < sc.tile_count) load_cols(t + gridDim.x);
+      if (eok && !mbar_wait(&tmem_full[b], (tc >> 1) & 1)) {
+        if (lane == 0) atomicOr(err, kDevErrSpin);
+        eok = false;
+      }
+      if (!eok) continue;
       tc_fence_after();
       for (int c = 0; c < kTN; c += 32) {
         uint32_t v[32];
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + b * (uint32_t)kTN + (uint32_t)c, v);
         const int col0 = t * sc.tile_stride * kTN + c;
-        const int jl = col0 + lane;
-        const float njl = jl < n ? norms[jl] : 0.0f;
-        const float sjl = jl < n ? snorms[jl] : 0.0f;
-        float wjl = -inf;
-        if (kPass == 1 && jl < sc.n_exist) wjl = key_dist(sc.g_key[(size_t)jl * kListW + kListW - 1]);
+        float cmin = inf;  // pass 0: this chunk's smallest upper bound
 #pragma unroll 4
         for (int i = 0; i < 32; ++i) {
-          const float nj = __shfl_sync(0xffffffffu, njl, i);
-          const float sj = __shfl_sync(0xffffffffu, sjl, i);
+          const float nj = cn[c + i];
+          const float sj = cn[kTN + c + i];
           const int j = col0 + i;
           const float dv = __fsub_rn(__fadd_rn(nm, nj), __fmul_rn(2.0f, __uint_as_float(v[i])));
-          if (kKeepD) stg[lane * kStagePitch + i] = dv;
+          if (kKeepD && live && j < n) D[(long)m * ldD + j] = dv;
           const float bnd = pair_bound(sc.coef, sm, sj, nm, nj);
-          if (kPass <= 1) {
-            if (live && j < n && j != row) {
-              const float ub = fmaxf(__fadd_ru(dv, bnd), 0.0f);
-              if (ub < t_loc && ub <= seed) t_loc = heap_push(heap, hcnt, ub);
+          const bool other = live && j < n && j != row;
+          if (kPass == 0 && other) cmin = fminf(cmin, fmaxf(__fadd_ru(dv, bnd), 0.0f));
+          if (kPass == 1 && other) {
+            const float ub = fmaxf(__fadd_ru(dv, bnd), 0.0f);
+            if (ub < t_loc && ub <= seed) t_loc = heap_push(heap, hcnt, ub);
+          }
+          if (kPass == 3 && other) {
+            const float lb = __fsub_rd(dv, bnd);
+            if (lb <= seed) {
+              if (pcnt < sc.pre_cap) {
+                sc.pre[seg + pcnt] = ((unsigned long long)__float_as_uint(lb) << 32) | (unsigned)j;
+                sc.pre_ub[seg + pcnt] = fmaxf(__fadd_ru(dv, bnd), 0.0f);
+              }
+              ++pcnt;
             }
           }
-          if (kPass == 1) {
-            const float wj = __shfl_sync(0xffffffffu, wjl, i);
+          if (col_test) {
+            const float wj = cn[2 * kTN + c + i];
             const bool hit = live && j < sc.n_exist && __fsub_rd(dv, bnd) <= wj;
             const unsigned bal = __ballot_sync(0xffffffffu, hit);
             if (bal) {
@@ -405,24 +499,18 @@ __global__ void __launch_bounds__(kExactThreads, 1)
             cand_m[atomicAdd(&sc.row_cnt[m], 1)] = j;
           }
         }
-        if (kKeepD) {
-          __syncwarp();
-          if (col0 + lane < n) {
-#pragma unroll 4
-            for (int rr = 0; rr < 32; ++rr) {
-              const int mrow = m0 + quarter * 32 + rr;
-              if (mrow < nb) D[(long)mrow * ldD + col0 + lane] = stg[rr * kStagePitch + lane];
-            }
-          }
-          __syncwarp();
-        }
+        if (kPass == 0 && live) sc.mins[(size_t)m * sc.mins_ld + t * (kTN / 32) + c / 32] = cmin;
       }
       tc_fence_before();
       mbar_arrive(&tmem_empty[b]);
     }
-    if (kPass <= 1 && live) {
+    if (kPass == 1 && live) {
       float *out = sc.heaps + ((size_t)m * gridDim.x + blockIdx.x) * kListTop;
       for (int i = 0; i < kListTop; ++i) out[i] = i < hcnt ? heap[i * kTM] : inf;
+    }
+    if (kPass == 3 && live) {
+      sc.pre_cnt[(size_t)m * gridDim.x + blockIdx.x] = min(pcnt, sc.pre_cap);
+      if (pcnt > sc.pre_cap) atomicOr(sc.pre_over, 1);
     }
   }
   tc_fence_before();
@@ -459,38 +547,133 @@ constexpr int kTile = 32;
 constexpr int kTileLd = 33;
 constexpr int kFinalWarps = 4;
 
+// Merges each lane's value u into the warp's ascending top 32 (lane l holds
+// the l-th smallest); values not below the current 32nd change nothing.
+GM_D void top32_merge(float &top, float u, int lane) {
+  unsigned pend = __ballot_sync(0xffffffffu, u < __shfl_sync(0xffffffffu, top, 31));
+  while (pend) {
+    const int src = __ffs(pend) - 1;
+    pend &= pend - 1;
+    const float x = __shfl_sync(0xffffffffu, u, src);
+    const unsigned pos_mask = __ballot_sync(0xffffffffu, x < top);
+    if (!pos_mask) continue;
+    const int pos = __ffs(pos_mask) - 1;
+    const float prev = __shfl_up_sync(0xffffffffu, top, 1);
+    if (lane > pos) top = prev;
+    else if (lane == pos) top = x;
+  }
+}
+
+// The 32nd smallest of cnt values at v (inf when fewer than 32 are finite),
+// one warp; eight 32-value chunks are loaded together, then merged.
+GM_D float warp_32nd(const float *v, int cnt, int lane) {
+  const float inf = __int_as_float(0x7f800000);
+  float top = inf;
+  for (int c0 = 0; c0 < cnt; c0 += 8 * 32) {
+    float u[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int idx = c0 + q * 32 + lane;
+      u[q] = idx < cnt ? v[idx] : inf;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) top32_merge(top, u[q], lane);
+  }
+  return __shfl_sync(0xffffffffu, top, 31);
+}
+
+// Warp per batch row: T = the 32nd smallest of the union of the CTAs' heaps
+// (pass 1), capped by the seed; both bound the row's 32nd smallest upper
+// bound from above.  With run_if, only when *run_if != 0.
 __global__ void __launch_bounds__(kFinalWarps * 32)
     k_row_threshold(const float *heaps, int ncta, int nrows, int n, const float *seed, float *row_t,
-                    unsigned long long *stat) {
+                    const int *run_if, unsigned long long *stat) {
+  if (run_if && *run_if == 0) return;
   const int lane = threadIdx.x & 31;
   const int ml = blockIdx.x * kFinalWarps + (threadIdx.x >> 5);
   if (ml >= nrows) return;
   const float inf = __int_as_float(0x7f800000);
-  const float *h = heaps + (size_t)ml * ncta * kListTop;
-  const int cnt = ncta * kListTop;
-  // the 32 smallest upper bounds of the union, ascending across the lanes
-  float top = inf;
-  for (int c0 = 0; c0 < cnt; c0 += 32) {
-    const float u = c0 + lane < cnt ? h[c0 + lane] : inf;
-    unsigned pend = __ballot_sync(0xffffffffu, u < __shfl_sync(0xffffffffu, top, 31));
-    while (pend) {
-      const int src = __ffs(pend) - 1;
-      pend &= pend - 1;
-      const float x = __shfl_sync(0xffffffffu, u, src);
-      const unsigned pos_mask = __ballot_sync(0xffffffffu, x < top);
-      if (!pos_mask) continue;
-      const int pos = __ffs(pos_mask) - 1;
-      const float prev = __shfl_up_sync(0xffffffffu, top, 1);
-      if (lane > pos) top = prev;
-      else if (lane == pos) top = x;
-    }
-  }
-  // the 32nd smallest of the union (inf when it holds fewer than 32), capped
-  // by the seed: both bound the row's 32nd smallest upper bound from above
-  const float T = fminf(__shfl_sync(0xffffffffu, top, 31), seed ? seed[ml] : inf);
+  const float T = fminf(warp_32nd(heaps + (size_t)ml * ncta * kListTop, ncta * kListTop, lane),
+                        seed ? seed[ml] : inf);
   if (lane == 0) {
     // fewer than 32 other rows: every column is a candidate
     row_t[ml] = n - 1 < kListTop ? inf : T;
+    if (stat) atomicAdd(&stat[5], (unsigned long long)n);
+  }
+}
+
+// Warp per batch row: the seed, the 32nd smallest of the row's chunk minima
+// from pass 0 (the largest upper bound of 32 distinct columns).
+__global__ void __launch_bounds__(kFinalWarps * 32)
+    k_seed_select(const float *mins, int mins_ld, int nrows, float *seed) {
+  const int lane = threadIdx.x & 31;
+  const int ml = blockIdx.x * kFinalWarps + (threadIdx.x >> 5);
+  if (ml >= nrows) return;
+  const float T = warp_32nd(mins + (size_t)ml * mins_ld, mins_ld, lane);
+  if (lane == 0) seed[ml] = T;
+}
+
+// Warp per batch row, after pass 3: T = the 32nd smallest stored upper
+// bound (exact: every column whose upper bound is at most T was stored),
+// then the row's candidates, the stored columns with lower bound <= T.  Lane
+// l walks segments l, l + 32, ...; entry i of every lane's segment is
+// handled together (four entries loaded ahead).  Does nothing when a segment
+// overflowed (the heap passes then run instead).
+__global__ void __launch_bounds__(kFinalWarps * 32)
+    k_pre_select(const unsigned long long *pre, const float *pre_ub, const int *pre_cnt, int gx,
+                 int cap, const int *pre_over, int nrows, int n, float *row_t, int *cand,
+                 long cand_ld, int *row_cnt, unsigned long long *stat) {
+  if (*pre_over) {
+    if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stat[9], 1ull);
+    return;
+  }
+  const int lane = threadIdx.x & 31;
+  const int m = blockIdx.x * kFinalWarps + (threadIdx.x >> 5);
+  if (m >= nrows) return;
+  const float inf = __int_as_float(0x7f800000);
+  float top = inf;
+  for (int c0 = 0; c0 < gx; c0 += 32) {
+    const int c = c0 + lane;
+    const size_t seg = (size_t)m * gx + c;
+    const int len = c < gx ? pre_cnt[seg] : 0;
+    const float *u = pre_ub + seg * (size_t)cap;
+    int maxlen = len;
+    for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
+    for (int i0 = 0; i0 < maxlen; i0 += 4) {
+      float v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = i0 + q < len ? u[i0 + q] : inf;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) top32_merge(top, v[q], lane);
+    }
+  }
+  // fewer than 32 other rows: every column is a candidate
+  const float T = n - 1 < kListTop ? inf : __shfl_sync(0xffffffffu, top, 31);
+  int *out = cand + (long)m * cand_ld;
+  int cnt = 0;
+  for (int c0 = 0; c0 < gx; c0 += 32) {
+    const int c = c0 + lane;
+    const size_t seg = (size_t)m * gx + c;
+    const int len = c < gx ? pre_cnt[seg] : 0;
+    const unsigned long long *e = pre + seg * (size_t)cap;
+    int maxlen = len;
+    for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
+    for (int i0 = 0; i0 < maxlen; i0 += 4) {
+      unsigned long long v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) v[q] = i0 + q < len ? e[i0 + q] : 0ull;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const bool keep = i0 + q < len && __uint_as_float((unsigned)(v[q] >> 32)) <= T;
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (keep) out[cnt + __popc(bal & ((1u << lane) - 1u))] = (int)(unsigned)v[q];
+        cnt += __popc(bal);
+      }
+    }
+  }
+  if (lane == 0) {
+    row_t[m] = T;
+    row_cnt[m] = cnt;
     if (stat) atomicAdd(&stat[5], (unsigned long long)n);
   }
 }
@@ -776,7 +959,8 @@ void launch_to_bf16(const DevState &st, void *xh, int dh, int row0, int nrows, c
 template <int kPass, bool kKeepD>
 static void launch_tile(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
                         int nrows, int n, const ExactScreen &x, long ldD, int gx, int m_tiles,
-                        int tile_count, int tile_stride, const float *seed, cudaStream_t s) {
+                        int tile_count, int tile_stride, const float *seed, int pre_cap,
+                        int mins_ld, int col_test, const int *run_if, cudaStream_t s) {
   // once per device (sessions on several host threads may launch at once)
   static std::atomic<unsigned> configured{0u};
   int dev = 0;
@@ -794,6 +978,15 @@ static void launch_tile(const DevState &st, const ExactMaps &maps, int dh, int r
   sc.tile_stride = tile_stride;
   sc.heaps = x.heaps;
   sc.seed = seed;
+  sc.mins = x.mins;
+  sc.mins_ld = mins_ld;
+  sc.pre = x.pre;
+  sc.pre_ub = x.pre_ub;
+  sc.pre_cnt = x.pre_cnt;
+  sc.pre_cap = pre_cap;
+  sc.pre_over = x.pre_over;
+  sc.col_test = col_test;
+  sc.run_if = run_if;
   sc.row_t = x.row_t;
   sc.cand = x.cand;
   sc.cand_ld = ldD;
@@ -810,38 +1003,67 @@ static void launch_tile(const DevState &st, const ExactMaps &maps, int dh, int r
   note_launch();
 }
 
-// Column tiles of the seed pass (evenly spaced over the columns).
+// Column tiles of the seed pass (evenly spaced over the columns): at least
+// 16, and one in 16 of the block's tiles, so that the seed stays a low
+// quantile of the row's upper bounds at any column count.
 constexpr int kSeedTiles = 16;
+constexpr int kSeedEvery = 16;
+
+int exact_seed_tiles(int n_tiles) { return std::max(kSeedTiles, n_tiles / kSeedEvery); }
 
 void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
                        int nrows, int n, const ExactScreen &x, long ldD, bool keep_d, int sms,
                        cudaStream_t s) {
-  if (nrows <= 0 || n <= 0) return;
-  const int m_tiles = cdiv(nrows, kTM);
   const int n_tiles = cdiv(n, kTN);
+  const int m_tiles = cdiv(nrows, kTM);
+  // CTAs per row tile so that the grid covers the SMs once
   const int gx = std::max(1, std::min(n_tiles, std::max(1, sms / m_tiles)));
+  const bool kd = keep_d && x.D;
   cudaMemsetAsync(x.row_cnt, 0, (size_t)nrows * sizeof(int), s);
   cudaMemsetAsync(x.counter, 0, sizeof(int), s);
-  const float *seed = nullptr;
-  if (n_tiles > 2 * kSeedTiles) {
-    // seed pass: the 32nd smallest upper bound over 16 spread tiles
-    const int stride = n_tiles / kSeedTiles;
-    const int gx0 = std::max(1, std::min(kSeedTiles, std::max(1, sms / m_tiles)));
-    launch_tile<0, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx0, m_tiles, kSeedTiles, stride,
-                          nullptr, s);
-    k_row_threshold<<<cdiv(nrows, kFinalWarps), kFinalWarps * 32, 0, s>>>(x.heaps, gx0, nrows, n, nullptr,
-                                                                          x.seed, nullptr);
+  const int tiles = exact_seed_tiles(n_tiles);
+  if (n_tiles > 2 * kSeedTiles && x.pre && x.pre_cap > 0 && gx <= x.pre_gx &&
+      tiles * (kTN / 32) <= x.mins_ld) {
+    // seed pass over a spread sample of tiles, then the store pass
+    const int stride = n_tiles / tiles;
+    const int gx0 = std::max(1, std::min(tiles, std::max(1, sms / m_tiles)));
+    const int mins_ld = tiles * (kTN / 32);
+    launch_tile<0, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx0, m_tiles, tiles, stride,
+                          nullptr, 0, mins_ld, 0, nullptr, s);
+    k_seed_select<<<cdiv(nrows, kFinalWarps), kFinalWarps * 32, 0, s>>>(x.mins, mins_ld, nrows, x.seed);
+    cudaMemsetAsync(x.pre_over, 0, sizeof(int), s);
+    if (kd)
+      launch_tile<3, true>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, x.seed,
+                           x.pre_cap, 0, 0, nullptr, s);
+    else
+      launch_tile<3, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, x.seed,
+                            x.pre_cap, 0, 0, nullptr, s);
+    k_pre_select<<<cdiv(nrows, kFinalWarps), kFinalWarps * 32, 0, s>>>(
+        x.pre, x.pre_ub, x.pre_cnt, gx, x.pre_cap, x.pre_over, nrows, n, x.row_t, x.cand, ldD, x.row_cnt,
+        st.stat);
+    note_launch(2);
+    // after an overflow only: the heap pass (seed-capped; its pairs were
+    // already pooled), the threshold and the candidate pass
+    launch_tile<1, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, x.seed, 0,
+                          0, 0, x.pre_over, s);
+    k_row_threshold<<<cdiv(nrows, kFinalWarps), kFinalWarps * 32, 0, s>>>(x.heaps, gx, nrows, n, x.seed,
+                                                                          x.row_t, x.pre_over, st.stat);
     note_launch();
-    seed = x.seed;
+    launch_tile<2, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, nullptr, 0,
+                          0, 0, x.pre_over, s);
+    return;
   }
-  if (keep_d && x.D)
-    launch_tile<1, true>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, seed, s);
+  if (kd)
+    launch_tile<1, true>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, nullptr, 0,
+                         0, 1, nullptr, s);
   else
-    launch_tile<1, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, seed, s);
-  k_row_threshold<<<cdiv(nrows, kFinalWarps), kFinalWarps * 32, 0, s>>>(x.heaps, gx, nrows, n, seed,
-                                                                        x.row_t, st.stat);
+    launch_tile<1, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, nullptr, 0,
+                          0, 1, nullptr, s);
+  k_row_threshold<<<cdiv(nrows, kFinalWarps), kFinalWarps * 32, 0, s>>>(x.heaps, gx, nrows, n, nullptr,
+                                                                        x.row_t, nullptr, st.stat);
   note_launch();
-  launch_tile<2, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, nullptr, s);
+  launch_tile<2, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, nullptr, 0,
+                        0, 0, nullptr, s);
 }
 
 void launch_exact_screen(const DevState &st, int row0, int blk0, int nrows, int n,

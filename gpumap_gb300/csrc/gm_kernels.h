@@ -113,6 +113,16 @@ struct ExactScreen {
   float *heaps = nullptr;     // rows x CTAs x 32: per-CTA smallest upper bounds (pass 1)
   float *row_t = nullptr;     // rows exact thresholds
   float *seed = nullptr;      // rows thresholds from the seed pass
+  float *mins = nullptr;       // rows x mins_ld chunk minima of the seed pass
+  int mins_ld = 0;
+  // stored columns of the store pass: rows x pre_gx segments of pre_cap packed
+  // (lower bound, column) entries and their upper bounds, the segments'
+  // lengths, and an overflow flag
+  unsigned long long *pre = nullptr;
+  float *pre_ub = nullptr;
+  int *pre_cnt = nullptr;
+  int pre_cap = 0, pre_gx = 0;
+  int *pre_over = nullptr;
   int *pool_j = nullptr, *pool_m = nullptr;    // column pairs as found
   int *pool_j2 = nullptr, *pool_m2 = nullptr;  // grouped by existing row
   float *pool_d = nullptr;    // their canonical distances
@@ -127,6 +137,8 @@ struct ExactScreen {
 // per-row exact threshold, then the candidates): candidate columns per batch
 // row and (existing row, batch row) pairs land in x.  With keep_d the
 // approximate tile is also written to x.D (nrows x ldD), for tests.
+// Column tiles the seed pass samples out of n_tiles.
+int exact_seed_tiles(int n_tiles);
 void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int row0, int blk0,
                        int nrows, int n, const ExactScreen &x, long ldD, bool keep_d, int sms,
                        cudaStream_t s);

@@ -106,6 +106,8 @@ typedef struct gm_stats {
   uint64_t exact_pairs;       /* batch x column pairs formed on the tensor cores */
   uint64_t exact_rescored;    /* pairs re-scored in FP32 */
   double phase_s[3];          /* insertion / update / embedding seconds */
+  uint64_t exact_overflow_blocks; /* insertion blocks whose stored candidates overflowed, so
+                                     that the candidate pass over the tiles ran again */
 } gm_stats;
 
 /* Replaces GPUMAPParams() defaults (gpumap.cuh:15-30). */

@@ -45,6 +45,12 @@ int gm_debug_copy(const struct gm_session *s, int which, void *host, uint64_t by
  * approximate distance tile for GM_BUF_EXACT_D.  Off by default: the screen
  * runs as the tile leaves the tensor memory and the tile is not stored. */
 int gm_debug_keep_tiles(struct gm_session *s, int on);
+/* Precision 1: entries per segment of stored columns that the store pass
+ * over the tiles may keep (clamped to the 64 allocated; 0 runs the heap and
+ * candidate passes instead, as for blocks of up to 32 column tiles).  A
+ * segment that would exceed it makes the heap and candidate passes run for
+ * its block (gm_stats.exact_overflow_blocks). */
+int gm_debug_pre_capacity(struct gm_session *s, int cap);
 /* Host and device scalars, out[0..n):
  *  0 n_inserted, 1 insertion-queue head, 2 new-row embedding-queue head,
  *  3 embedding cursor (-1 = none), 4 embedding sweeps, 5 last nnz,

@@ -278,6 +278,40 @@ def test_exact_mode_bitexact(native, oracle_mod, d, metric, k):
     assert recall_at_k(idx, ei) > 0.99
 
 
+@pytest.mark.parametrize("cap", [None, 1, 0])
+def test_exact_mode_seeded_screen_bitexact(native, oracle_mod, cap):
+    # past 32 column tiles (8,192 rows) the tile screen seeds each row's
+    # threshold from the chunk minima of a spread sample of tiles and stores
+    # every column the seed admits in one full pass; cap 1 makes the stored
+    # segments overflow, so the heap and candidate passes run for the block;
+    # cap 0 runs those passes instead of the store pass.  Lists are the
+    # oracle's bit for bit in every case, with large (3,000-row) and small
+    # (500-row) insertion batches
+    n, d, k = 12000, 32, 15
+    X, _ = gaussian_mixture(n, d, seed=21)
+    s = native.Session(native.default_params(n_instances=n, n_features=d, n_neighbors=k, max_epoch=10,
+                                             device=0, precision=1))
+    if cap is not None:
+        s.pre_capacity(cap)
+    s.set_stats(True)
+    o = oracle_mod.OracleSession(n, d, k=k, max_epoch=10, precision=1)
+    c0 = 0
+    for rows in [3000, 3000, 3000, 500, 500, 500, 500, 500, 500]:
+        chunk = X[c0 : c0 + rows]
+        c0 += rows
+        s.append_host(chunk)
+        o.append(chunk)
+        same_result(s.run(rows, 0, 200), o.run(rows, 0, 200))
+        same_state(s, o, tag=f"rows {c0}")
+    same_state(s, o, embed=True, tag="final")
+    over = s.stats().exact_overflow_blocks
+    # seeded blocks: the cycles at 9,000 rows and after (7 of them)
+    if cap == 1:
+        assert over == 7, over
+    else:
+        assert over == 0, over
+
+
 # ---------------------------------------------------------------------------
 # overlap = 1: each cycle's embedding runs on its own stream beside the next
 # cycle's distance work; everything the oracle pins must be unchanged

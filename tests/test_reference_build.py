@@ -7,12 +7,13 @@ two of its runs already differ; the comparisons are of what both must share:
 
 * the stored distance of every listed pair is the metric's distance of that
   pair (squared L2; 2 (1 - cos) for cosine) in both builds, to FP32 rounding;
-* every published slot of this build is filled after insertion; the
-  reference leaves some rows' slots unfilled (id UINT_MAX, dist FLT_MAX) on
-  this schedule, so the quality comparisons are one-sided: recall@k of the
-  plain path (precision 0, the reference's algorithm) is at least the
-  reference's minus 0.05, trustworthiness at least the reference's minus
-  0.03, and the precision form's lists are exact.
+* both keep the random-init placeholders (a valid id at FLT_MAX) that no
+  candidate displaced -- the forward merge has no effect below 256 valid
+  candidates, in the reference and here -- so the fractions of such slots
+  agree within 0.05;
+* recall@k of the plain path (precision 0, the reference's algorithm) is at
+  least the reference's minus 0.05, trustworthiness at least the
+  reference's minus 0.03, and the precision form's lists are exact.
 
 Skipped when the reference build is absent.
 """
@@ -92,8 +93,7 @@ def test_plain_path_agrees_with_reference_build(native, metric, n, d, seed):
     # stored distance convention, pinned to the reference's own output
     r_ok = (r_ids >= 0) & (r_ids < n) & (r_dist < 1e30)
     o_ok = (o_ids >= 0) & (o_ids < n) & (o_dist < 1e30)
-    assert o_ok.all(), np.flatnonzero(~o_ok.all(1))[:10]
-    assert r_ok.mean() > 0.5, r_ok.mean()
+    assert abs(r_ok.mean() - o_ok.mean()) <= 0.05, (r_ok.mean(), o_ok.mean())
     for ids, dist, ok in ((r_ids, r_dist, r_ok), (o_ids, o_dist, o_ok)):
         want = _pair_dists(X, np.where(ok, ids, 0), metric)
         err = np.abs(dist.astype(np.float64) - want)[ok]
@@ -103,7 +103,7 @@ def test_plain_path_agrees_with_reference_build(native, metric, n, d, seed):
     ex, _ = exact_knn(X, k, queries=q, metric=metric)
     rec_r = recall_at_k(r_ids[q], ex)
     rec_o = recall_at_k(o_ids[q], ex)
-    assert rec_o >= rec_r - 0.05, (rec_o, rec_r, 1.0 - r_ok.mean())
+    assert rec_o >= rec_r - 0.05, (rec_o, rec_r)
 
     sample = np.arange(0, n, 6)
     t_r = trustworthiness(X, r_emb, k, sample=sample)

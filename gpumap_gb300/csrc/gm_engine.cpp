@@ -68,8 +68,9 @@ Session::Session(const gm_params &p) : p_(p) {
     int lo = 0, hi = 0;
     ck(cudaDeviceGetStreamPriorityRange(&lo, &hi), "stream priorities");
     ck(cudaStreamCreateWithPriority(&estream_, cudaStreamNonBlocking, hi), "cudaStreamCreate");
-    ck(cudaEventCreateWithFlags(&ev_pub_, cudaEventDisableTiming), "cudaEventCreate");
-    ck(cudaEventCreateWithFlags(&ev_emb_, cudaEventDisableTiming), "cudaEventCreate");
+    ck(cudaStreamCreateWithPriority(&estream_alt_, cudaStreamNonBlocking, hi), "cudaStreamCreate");
+    for (cudaEvent_t *e : {&ev_pub_, &ev_emb_, &ev_snap_, &ev_init_, &ev_hpin_, &ev_hpin_alt_})
+      ck(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "cudaEventCreate");
   }
 
   const size_t N = p.n_instances, d = p.n_features, k = p.n_neighbors;
@@ -122,26 +123,37 @@ Session::Session(const gm_params &p) : p_(p) {
     d_tmp_ = (int *)dalloc(std::max(scan_tmp_ints((int)Nm), compact_tmp_ints((int)Nm)) *
                            sizeof(int) + 64);
 
-    es_.flag = (int *)dalloc(Nm * sizeof(int));
-    es_.unsel = (int *)dalloc(Nm * sizeof(int));
-    es_.sigma = (float *)dalloc(Nm * sizeof(float));
-    es_.rho = (float *)dalloc(Nm * sizeof(float));
-    es_.deg = (int *)dalloc(Nm * sizeof(int));
-    es_.snap = (float *)dalloc(Nm * 2 * sizeof(float));
-    es_.fscal = (float *)dalloc(16 * sizeof(float));
-    es_.iscal = (int *)dalloc(16 * sizeof(int));
-    es_.cap_partial = (Nm * k + 255) / 256 + 512;
-    es_.partial = (float *)dalloc(es_.cap_partial * 2 * sizeof(float));
-    es_.ipartial = (int *)dalloc(es_.cap_partial * sizeof(int));
     // the embedding phase has its own batch, scan scratch, counters and
-    // pinned staging, so that it can run beside the other phases
-    es_.batch = (int *)dalloc(Nm * sizeof(int));
-    es_.tmp = (int *)dalloc(std::max(scan_tmp_ints((int)Nm), compact_tmp_ints((int)Nm)) *
+    // pinned staging, so that it can run beside the other phases (two sets
+    // in overlap mode, one per side)
+    auto alloc_side = [&](EmbedScratch &e, int *&cnt) {
+      e.flag = (int *)dalloc(Nm * sizeof(int));
+      e.unsel = (int *)dalloc(Nm * sizeof(int));
+      e.sigma = (float *)dalloc(Nm * sizeof(float));
+      e.rho = (float *)dalloc(Nm * sizeof(float));
+      e.deg = (int *)dalloc(Nm * sizeof(int));
+      e.snap = (float *)dalloc(Nm * 2 * sizeof(float));
+      e.fscal = (float *)dalloc(16 * sizeof(float));
+      e.iscal = (int *)dalloc(16 * sizeof(int));
+      e.cap_partial = (Nm * k + 255) / 256 + 512;
+      e.partial = (float *)dalloc(e.cap_partial * 2 * sizeof(float));
+      e.ipartial = (int *)dalloc(e.cap_partial * sizeof(int));
+      e.batch = (int *)dalloc(Nm * sizeof(int));
+      e.tmp = (int *)dalloc(std::max(scan_tmp_ints((int)Nm), compact_tmp_ints((int)Nm)) *
                             sizeof(int) + 64);
-    es_cnt_ = (int *)dalloc(16 * sizeof(int));
+      if (p.overlap) {
+        e.pub_idx_snap = (uint32_t *)dalloc(Nm * (k + 1) * sizeof(uint32_t));
+        e.pub_dist_snap = (float *)dalloc(Nm * (k + 1) * sizeof(float));
+      }
+      cnt = (int *)dalloc(16 * sizeof(int));
+    };
+    alloc_side(es_, es_cnt_);
+    if (p.overlap) alloc_side(es_alt_, es_cnt_alt_);
 
     ck(cudaMallocHost((void **)&h_pin_, (Nm + 64) * sizeof(uint32_t)), "cudaMallocHost");
     ck(cudaMallocHost((void **)&h_emb_pin_, (Nm + 64) * sizeof(uint32_t)), "cudaMallocHost");
+    if (p.overlap)
+      ck(cudaMallocHost((void **)&h_emb_pin_alt_, (Nm + 64) * sizeof(uint32_t)), "cudaMallocHost");
     if (p.precision == 1) {
       // split-BF16 shadow rows (hi | lo, 2 x dh bf16 each) plus a block of
       // candidate / pair scratch sized so that a block holds at most ~256 MB
@@ -186,6 +198,7 @@ Session::Session(const gm_params &p) : p_(p) {
     allocs_.clear();
     if (h_pin_) cudaFreeHost(h_pin_);
     if (h_emb_pin_) cudaFreeHost(h_emb_pin_);
+    if (h_emb_pin_alt_) cudaFreeHost(h_emb_pin_alt_);
     release_streams();
     throw;
   }
@@ -208,10 +221,13 @@ Session::Session(const gm_params &p) : p_(p) {
   ck(cudaMemsetAsync(st_.err, 0, 16, s), "memset");
   ck(cudaMemsetAsync(d_stat_, 0, 16 * sizeof(unsigned long long), s), "memset");
   ck(cudaMemsetAsync(us_.sizes, 0, Nm * sizeof(int4), s), "memset");
-  ck(cudaMemsetAsync(es_.sigma, 0, Nm * sizeof(float), s), "memset");
-  ck(cudaMemsetAsync(es_.rho, 0, Nm * sizeof(float), s), "memset");
-  ck(cudaMemsetAsync(es_.iscal, 0, 16 * sizeof(int), s), "memset");
-  ck(cudaMemsetAsync(es_.fscal, 0, 16 * sizeof(float), s), "memset");
+  for (EmbedScratch *e : {&es_, &es_alt_}) {
+    if (!e->sigma) continue;
+    ck(cudaMemsetAsync(e->sigma, 0, Nm * sizeof(float), s), "memset");
+    ck(cudaMemsetAsync(e->rho, 0, Nm * sizeof(float), s), "memset");
+    ck(cudaMemsetAsync(e->iscal, 0, 16 * sizeof(int), s), "memset");
+    ck(cudaMemsetAsync(e->fscal, 0, 16 * sizeof(float), s), "memset");
+  }
   if (xh_) ck(cudaMemsetAsync(xh_, 0, Nm * (size_t)dh_ * 4, s), "memset");
   ck(cudaGetLastError(), "init fill");
   ck(cudaStreamSynchronize(s), "init sync");
@@ -223,26 +239,47 @@ Session::Session(const gm_params &p) : p_(p) {
       h_pin_ = nullptr;
       cudaFreeHost(h_emb_pin_);
       h_emb_pin_ = nullptr;
+      if (h_emb_pin_alt_) cudaFreeHost(h_emb_pin_alt_);
+      h_emb_pin_alt_ = nullptr;
       release_streams();
       throw Error(GM_ERR_CUDA, "cuTensorMapEncodeTiled unavailable or failed");
     }
   }
   upd_q_.reset(N);
-  ensure_embed(1);
+  ensure_embed(es_, 1);
+  if (p.overlap) ensure_embed(es_alt_, 1);
 }
 
 void Session::release_streams() {
-  if (ev_pub_) cudaEventDestroy(ev_pub_);
-  if (ev_emb_) cudaEventDestroy(ev_emb_);
-  if (estream_) cudaStreamDestroy(estream_);
-  if (stream_) cudaStreamDestroy(stream_);
-  ev_pub_ = ev_emb_ = nullptr;
-  estream_ = stream_ = nullptr;
+  for (cudaEvent_t *e : {&ev_pub_, &ev_emb_, &ev_snap_, &ev_init_, &ev_hpin_, &ev_hpin_alt_}) {
+    if (*e) cudaEventDestroy(*e);
+    *e = nullptr;
+  }
+  for (cudaStream_t *q : {&estream_, &estream_alt_, &stream_}) {
+    if (*q) cudaStreamDestroy(*q);
+    *q = nullptr;
+  }
+}
+
+// Waits for both embedding sides.
+void Session::sync_embed_streams() {
+  for (cudaStream_t q : {estream_, estream_alt_})
+    if (q) ck(cudaStreamSynchronize(q), "cudaStreamSynchronize");
+}
+
+void Session::free_embed(EmbedScratch &e) {
+  if (!e.coo_row) return;
+  for (void *q : {(void *)e.coo_row, (void *)e.coo_col, (void *)e.coo_val, (void *)e.t_row,
+                  (void *)e.t_col, (void *)e.flag_tail, (void *)e.t_val, (void *)e.next_s,
+                  (void *)e.next_n, (void *)e.tmp2})
+    cudaFree(q);
+  e.coo_row = nullptr;
+  e.cap_coo = 0;
 }
 
 Session::~Session() {
-  if (stream_) cudaStreamSynchronize(stream_);
-  if (estream_) cudaStreamSynchronize(estream_);
+  for (cudaStream_t q : {stream_, estream_, estream_alt_})
+    if (q) cudaStreamSynchronize(q);
   for (auto &e : ev_pool_) cudaEventDestroy(e);
   for (auto &pr : ev_pending_) {
     cudaEventDestroy(pr.a);
@@ -252,20 +289,11 @@ Session::~Session() {
   if (cand_) cudaFree(cand_);
   if (cand_cnt_) cudaFree(cand_cnt_);
   if (cand_dist_) cudaFree(cand_dist_);
-  if (es_.coo_row) {
-    cudaFree(es_.coo_row);
-    cudaFree(es_.coo_col);
-    cudaFree(es_.coo_val);
-    cudaFree(es_.t_row);
-    cudaFree(es_.t_col);
-    cudaFree(es_.flag_tail);
-    cudaFree(es_.t_val);
-    cudaFree(es_.next_s);
-    cudaFree(es_.next_n);
-    cudaFree(es_.tmp2);
-  }
+  free_embed(es_);
+  free_embed(es_alt_);
   if (h_pin_) cudaFreeHost(h_pin_);
   if (h_emb_pin_) cudaFreeHost(h_emb_pin_);
+  if (h_emb_pin_alt_) cudaFreeHost(h_emb_pin_alt_);
   if (cstream_) cudaStreamSynchronize(cstream_);
   for (auto &slot : ring_) {
     if (slot.done) cudaEventDestroy(slot.done);
@@ -281,7 +309,7 @@ void Session::sync() { ck(cudaStreamSynchronize(stream_), "cudaStreamSynchronize
 // the main and the embedding streams; the main stream already waits for
 // every row transfer.
 void Session::order_after(cudaStream_t consumer) const {
-  for (cudaStream_t producer : {stream_, estream_}) {
+  for (cudaStream_t producer : {stream_, estream_, estream_alt_}) {
     if (!producer) continue;
     cudaEvent_t ev = nullptr;
     ck(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
@@ -296,8 +324,8 @@ void Session::order_after(cudaStream_t consumer) const {
 // reports a device error bit raised meanwhile.
 void Session::drain() {
   sync();
-  if (estream_) ck(cudaStreamSynchronize(estream_), "cudaStreamSynchronize");
-  emb_pending_ = false;
+  sync_embed_streams();
+  emb_pending_ = snap_pending_ = init_wait_ = false;
   check_device_error("embedding");
 }
 
@@ -351,8 +379,8 @@ void Session::set_keep_tile(bool on) {
 size_t Session::device_bytes() const {
   size_t b = fixed_bytes_;
   b += cand_rows_ * (size_t)kMaxCand * (sizeof(int) + sizeof(float)) + cand_rows_ * sizeof(int);
-  if (es_.coo_row)
-    b += es_.cap_coo * 9 * 4 + (compact_tmp_ints((int)es_.cap_coo) + 64) * sizeof(int);
+  for (const EmbedScratch *e : {&es_, &es_alt_})
+    if (e->coo_row) b += e->cap_coo * 9 * 4 + (compact_tmp_ints((int)e->cap_coo) + 64) * sizeof(int);
   return b;
 }
 
@@ -365,40 +393,30 @@ size_t Session::growth_bytes(uint32_t n_ins, uint32_t n_emb) const {
   // an embedding batch takes the queued new rows plus the cursor's rows
   const size_t nb = std::max<size_t>(n_emb, n_inserted_ + n_ins - emb_new_head_);
   const size_t c = std::max<size_t>(2 * std::max<size_t>(nb, 1) * (size_t)st_.k, 4096);
-  if (n_emb > 0 && c > es_.cap_coo) g += c * 9 * 4 + (compact_tmp_ints((int)c) + 64) * sizeof(int);
+  // (in overlap mode the next phase runs on the other side)
+  const EmbedScratch &next = p_.overlap ? es_alt_ : es_;
+  if (n_emb > 0 && c > next.cap_coo) g += c * 9 * 4 + (compact_tmp_ints((int)c) + 64) * sizeof(int);
   return g;
 }
 
-void Session::ensure_embed(size_t nb) {
+void Session::ensure_embed(EmbedScratch &e, size_t nb) {
   const size_t need = 2 * std::max<size_t>(nb, 1) * (size_t)st_.k;
-  if (need <= es_.cap_coo) return;
+  if (need <= e.cap_coo) return;
   sync();
-  if (estream_) ck(cudaStreamSynchronize(estream_), "cudaStreamSynchronize");
-  if (es_.coo_row) {
-    cudaFree(es_.coo_row);
-    cudaFree(es_.coo_col);
-    cudaFree(es_.coo_val);
-    cudaFree(es_.t_row);
-    cudaFree(es_.t_col);
-    cudaFree(es_.flag_tail);
-    cudaFree(es_.t_val);
-    cudaFree(es_.next_s);
-    cudaFree(es_.next_n);
-    cudaFree(es_.tmp2);
-    es_.coo_row = nullptr;
-  }
+  sync_embed_streams();
+  free_embed(e);
   const size_t c = std::max(need, (size_t)4096);
-  ck(cudaMalloc(&es_.coo_row, c * sizeof(int)), "cudaMalloc coo");
-  ck(cudaMalloc(&es_.coo_col, c * sizeof(int)), "cudaMalloc coo");
-  ck(cudaMalloc(&es_.coo_val, c * sizeof(float)), "cudaMalloc coo");
-  ck(cudaMalloc(&es_.t_row, c * sizeof(int)), "cudaMalloc coo");
-  ck(cudaMalloc(&es_.t_col, c * sizeof(int)), "cudaMalloc coo");
-  ck(cudaMalloc(&es_.flag_tail, c * sizeof(int)), "cudaMalloc coo");
-  ck(cudaMalloc(&es_.t_val, c * sizeof(float)), "cudaMalloc coo");
-  ck(cudaMalloc(&es_.next_s, c * sizeof(float)), "cudaMalloc coo");
-  ck(cudaMalloc(&es_.next_n, c * sizeof(float)), "cudaMalloc coo");
-  ck(cudaMalloc(&es_.tmp2, (compact_tmp_ints((int)c) + 64) * sizeof(int)), "cudaMalloc coo");
-  es_.cap_coo = c;
+  ck(cudaMalloc(&e.coo_row, c * sizeof(int)), "cudaMalloc coo");
+  ck(cudaMalloc(&e.coo_col, c * sizeof(int)), "cudaMalloc coo");
+  ck(cudaMalloc(&e.coo_val, c * sizeof(float)), "cudaMalloc coo");
+  ck(cudaMalloc(&e.t_row, c * sizeof(int)), "cudaMalloc coo");
+  ck(cudaMalloc(&e.t_col, c * sizeof(int)), "cudaMalloc coo");
+  ck(cudaMalloc(&e.flag_tail, c * sizeof(int)), "cudaMalloc coo");
+  ck(cudaMalloc(&e.t_val, c * sizeof(float)), "cudaMalloc coo");
+  ck(cudaMalloc(&e.next_s, c * sizeof(float)), "cudaMalloc coo");
+  ck(cudaMalloc(&e.next_n, c * sizeof(float)), "cudaMalloc coo");
+  ck(cudaMalloc(&e.tmp2, (compact_tmp_ints((int)c) + 64) * sizeof(int)), "cudaMalloc coo");
+  e.cap_coo = c;
 }
 
 // ---------------------------------------------------------------------------
@@ -473,7 +491,7 @@ void Session::reset_stats() {
 
 void Session::get_stats(gm_stats *out) {
   sync();
-  if (estream_) ck(cudaStreamSynchronize(estream_), "cudaStreamSynchronize");
+  sync_embed_streams();
   collect_timings(true);
   unsigned long long h[16];
   ck(cudaMemcpy(h, d_stat_, sizeof(h), cudaMemcpyDeviceToHost), "stats");
@@ -561,6 +579,10 @@ gm_result Session::run(uint32_t n_ins, uint32_t n_upd, uint32_t n_emb) {
   gm_result r{};
   log("[GPUMAP] run() start: insert=%u update=%u embed=%u inserted=%zu\n", n_ins, n_upd, n_emb,
       n_inserted_);
+  // overlap mode: with no update in between, the new rows' embedding moves to
+  // the start of this run's embedding phase (it must follow the phase in
+  // flight, which the insertion itself need not wait for)
+  defer_init_ = p_.overlap && n_upd == 0 && n_emb != 0 && !emb_done_;
   if (!ins_done_) {
     const auto t0 = Clock::now();
     r.n_insertion_ops = insert(n_ins);
@@ -595,6 +617,8 @@ gm_result Session::run(uint32_t n_ins, uint32_t n_upd, uint32_t n_emb) {
     r.embedding_time = std::chrono::duration<float>(t1 - t0).count();
     log("[GPUMAP] embed done: actual=%u time=%.3fs\n", r.n_embedding_ops, r.embedding_time);
   }
+  flush_init();
+  defer_init_ = false;
   collect_timings(!p_.overlap);
   stats_.phase_s[0] += r.insertion_time;
   stats_.phase_s[1] += r.update_time;
@@ -633,6 +657,13 @@ uint32_t Session::insert(uint32_t n_ops) {
   }
   ck(cudaMemsetAsync(st_.dirty, 0, (size_t)n * sizeof(int), s), "dirty");
   launch_row_norms(st_, row0, nb, s);
+  // the previous insertion's rows get their embedding at the start of the
+  // embedding phase that followed it, from their working lists: no list
+  // changes before that has run
+  auto wait_init = [&] {
+    if (init_wait_) ck(cudaStreamWaitEvent(s, ev_init_, 0), "wait row embedding");
+    init_wait_ = false;
+  };
   if (p_.precision == 1) {
     // exact lists: every batch row against every inserted row on the tensor
     // cores, re-scored in FP32 where the split-BF16 bound cannot decide
@@ -645,6 +676,7 @@ uint32_t Session::insert(uint32_t n_ops) {
       timed_begin(3);
       launch_exact_dist(st_, maps_, dh_, row0, b0, rows, ncol, xs_, (long)ncol, keep_tile_, sms_, s);
       timed_end(3);
+      wait_init();
       timed_begin(4);
       launch_exact_screen(st_, row0, b0, rows, ncol, xs_, (long)ncol, sms_, s);
       timed_end(4);
@@ -656,6 +688,7 @@ uint32_t Session::insert(uint32_t n_ops) {
     }
   } else {
     ensure_cand(B);
+    wait_init();
     launch_random_init(st_, row0, nb, n, window_start, seed, s);
     for (int it = 0; it < kInsertIters; ++it) {
       launch_sample_candidates(st_, row0, nb, n, cand_, cand_cnt_, s);
@@ -668,14 +701,25 @@ uint32_t Session::insert(uint32_t n_ops) {
   }
   // existing rows whose list changed, ascending
   compact_flags(st_.dirty, row0, -1, d_rows_, d_cnt_, d_tmp_, s);
-  // the embedding still in flight reads the published table and writes the
-  // embedding that embed_init reads: publish only after it
-  if (emb_pending_) ck(cudaStreamWaitEvent(s, ev_emb_, 0), "wait embedding");
+  // the embedding phase in flight reads the published table until its
+  // snapshot (overlap mode) and the embedding until it ends
+  if (snap_pending_) ck(cudaStreamWaitEvent(s, ev_snap_, 0), "wait snapshot");
+  else if (emb_pending_) ck(cudaStreamWaitEvent(s, ev_emb_, 0), "wait embedding");
   launch_adopt_and_publish(st_, row0, nb, d_rows_, d_cnt_, row0, n, s);
-  launch_embed_init(st_, row0, nb, n, s);
+  if (defer_init_) {
+    // the new rows' embedding waits for the phase in flight; it runs at the
+    // start of this run's embedding phase
+    init_pending_ = nb > 0;
+    init_row0_ = (int)row0;
+    init_nb_ = nb;
+    init_n_ = (int)n;
+  } else {
+    if (emb_pending_) ck(cudaStreamWaitEvent(s, ev_emb_, 0), "wait embedding");
+    launch_embed_init(st_, row0, nb, n, s);
+  }
   ck(cudaMemcpyAsync(h_pin_, d_cnt_, sizeof(int), cudaMemcpyDeviceToHost, s), "count");
   sync();
-  emb_pending_ = false;  // the stream waited for it above
+  if (!defer_init_) emb_pending_ = snap_pending_ = false;  // the stream waited for it above
   const int nd = (int)h_pin_[0];
   if (nd > 0) {
     ck(cudaMemcpyAsync(h_pin_, d_rows_, (size_t)nd * sizeof(int), cudaMemcpyDeviceToHost, s),
@@ -695,8 +739,12 @@ uint32_t Session::update(uint32_t n_ops, size_t &changed) {
   changed = 0;
   const size_t n = n_inserted_;
   if (n_ops == 0 || upd_done_ || n == 0) return 0;
-  // the update republishes rows the embedding in flight reads
-  if (emb_pending_) ck(cudaStreamWaitEvent(stream_, ev_emb_, 0), "wait embedding");
+  // the update republishes rows the embedding in flight reads (until its
+  // snapshot in overlap mode) and changes working lists
+  if (snap_pending_) ck(cudaStreamWaitEvent(stream_, ev_snap_, 0), "wait snapshot");
+  else if (emb_pending_) ck(cudaStreamWaitEvent(stream_, ev_emb_, 0), "wait embedding");
+  if (init_wait_) ck(cudaStreamWaitEvent(stream_, ev_init_, 0), "wait row embedding");
+  init_wait_ = false;
   const size_t threshold = (size_t)(0.0001f * (float)n);
   uint32_t left = n_ops;
   while (left > 0) {
@@ -810,43 +858,88 @@ uint32_t Session::embed(uint32_t n_ops) {
   const int nb = (int)batch.size();
   const int ni = (int)n;
   const int k = st_.k;
-  // overlap: the phase runs on its own stream once the table it reads is
-  // published; a previous embedding still in flight finishes first (its
-  // staging buffer and scratch are reused)
-  if (emb_pending_) ck(cudaEventSynchronize(ev_emb_), "wait embedding");
   cudaStream_t s = stream_;
   if (p_.overlap) {
+    // this phase takes the other side (stream, scratch, staging); it reads
+    // the table the insertion just published
+    std::swap(estream_, estream_alt_);
+    std::swap(es_, es_alt_);
+    std::swap(es_cnt_, es_cnt_alt_);
+    std::swap(h_emb_pin_, h_emb_pin_alt_);
+    std::swap(ev_hpin_, ev_hpin_alt_);
     ck(cudaEventRecord(ev_pub_, stream_), "record publish");
     ck(cudaStreamWaitEvent(estream_, ev_pub_, 0), "wait publish");
     s = estream_;
+    // the side's staging was last read by the upload two phases ago
+    ck(cudaEventSynchronize(ev_hpin_), "staging");
   }
-  ensure_embed((size_t)nb);
+  ensure_embed(es_, (size_t)nb);
   std::memcpy(h_emb_pin_, batch.data(), (size_t)nb * sizeof(uint32_t));
   ck(cudaMemcpyAsync(es_.batch, h_emb_pin_, (size_t)nb * sizeof(int), cudaMemcpyHostToDevice, s),
      "batch");
+  if (p_.overlap) ck(cudaEventRecord(ev_hpin_, s), "record staging");
   const int euclid = p_.metric == GM_METRIC_EUCLIDEAN;
   const double target = std::log2((double)(k - 1));
   launch_fuzzy_graph(st_.pub_idx, st_.pub_dist, ni, k, euclid, es_.batch, nb, target, es_, s);
   if (sweeps_ > 2) emb_done_ = upd_done_;
   const uint64_t noise_seed = 42ull ^ (uint64_t)sweeps_;
-  launch_add_noise(st_.emb, ni, es_.batch, nb, 0.001f, noise_seed, es_, s);
-  launch_schedule(ni, nb, k, p_.alpha, (int)p_.max_epoch, (int)p_.negative_sample_rate, es_, s);
+  const int nu = ni - nb;
+  const uint32_t *heur_idx = st_.pub_idx;
+  const float *heur_dist = st_.pub_dist;
+  if (!p_.overlap) {
+    launch_add_noise(st_.emb, ni, es_.batch, nb, 0.001f, noise_seed, es_, s);
+    launch_schedule(ni, nb, k, p_.alpha, (int)p_.max_epoch, (int)p_.negative_sample_rate, es_, s);
+  } else {
+    // the fuzzy set and schedule read only the published table: they run
+    // beside the previous phase's SGD.  The reposition step reads the table
+    // as it is now (a snapshot: the next insertion may publish before it
+    // runs).  Noise, the new rows' embedding and the SGD read the embedding
+    // and wait for the previous phase.
+    launch_schedule(ni, nb, k, p_.alpha, (int)p_.max_epoch, (int)p_.negative_sample_rate, es_, s);
+    if (nu > 0) {
+      const size_t w = (size_t)ni * (size_t)(k + 1);
+      ck(cudaMemcpyAsync(es_.pub_idx_snap, st_.pub_idx, w * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
+                         s), "snapshot");
+      ck(cudaMemcpyAsync(es_.pub_dist_snap, st_.pub_dist, w * sizeof(float), cudaMemcpyDeviceToDevice,
+                         s), "snapshot");
+      heur_idx = es_.pub_idx_snap;
+      heur_dist = es_.pub_dist_snap;
+    }
+    ck(cudaEventRecord(ev_snap_, s), "record snapshot");
+    snap_pending_ = true;
+    if (emb_pending_) ck(cudaStreamWaitEvent(s, ev_emb_, 0), "wait embedding");
+    if (init_pending_) {
+      launch_embed_init(st_, init_row0_, init_nb_, init_n_, s);
+      ck(cudaEventRecord(ev_init_, s), "record row embedding");
+      init_pending_ = false;
+      init_wait_ = true;
+    }
+    launch_add_noise(st_.emb, ni, es_.batch, nb, 0.001f, noise_seed, es_, s);
+  }
   launch_set_int(es_.iscal + kIscalN, ni, s);
   timed_begin(2, s);
   run_sgd(s);
   timed_end(2, s);
-  const int nu = ni - nb;
   if (nu > 0) {
     ck(cudaMemsetAsync(es_.flag, 0, (size_t)ni * sizeof(int), s), "flags");
     launch_mark_rows(es_.batch, nb, es_.flag, s);
     compact_flags(es_.flag, ni, 0, es_.unsel, es_cnt_, es_.tmp, s);
-    launch_heuristic(st_.pub_idx, st_.pub_dist, ni, k, euclid, es_.unsel, nu, st_.emb, es_, s);
+    launch_heuristic(heur_idx, heur_dist, ni, k, euclid, es_.unsel, nu, st_.emb, es_, s);
   }
   if (p_.overlap) {
     ck(cudaEventRecord(ev_emb_, s), "record embedding");
     emb_pending_ = true;
   }
   return (uint32_t)nb;
+}
+
+// A deferred embedding of new rows whose phase did not run: on the main
+// stream, after the phase in flight.
+void Session::flush_init() {
+  if (!init_pending_) return;
+  if (emb_pending_) ck(cudaStreamWaitEvent(stream_, ev_emb_, 0), "wait embedding");
+  launch_embed_init(st_, init_row0_, init_nb_, init_n_, stream_);
+  init_pending_ = false;
 }
 
 // The max_epoch SGD epochs of one embedding call: one cooperative launch
@@ -869,8 +962,9 @@ void Session::run_sgd(cudaStream_t s) {
 void Session::close() {
   if (closed_) return;
   cudaStreamSynchronize(stream_);
-  if (estream_) cudaStreamSynchronize(estream_);
-  emb_pending_ = false;
+  for (cudaStream_t q : {estream_, estream_alt_})
+    if (q) cudaStreamSynchronize(q);
+  emb_pending_ = snap_pending_ = init_wait_ = false;
   closed_ = true;
 }
 
@@ -878,7 +972,8 @@ void Session::debug_scalars(int64_t *out, int cnt) const {
   int iscal[16] = {0};
   unsigned err = 0;
   cudaStreamSynchronize(stream_);
-  if (estream_) cudaStreamSynchronize(estream_);
+  for (cudaStream_t q : {estream_, estream_alt_})
+    if (q) cudaStreamSynchronize(q);
   cudaMemcpy(iscal, es_.iscal, sizeof(iscal), cudaMemcpyDeviceToHost);
   cudaMemcpy(&err, st_.err, sizeof(err), cudaMemcpyDeviceToHost);
   int64_t v[11] = {(int64_t)n_inserted_,

@@ -97,7 +97,10 @@ class Session {
   uint32_t embed(uint32_t n_ops);
   void check_device_error(const char *phase);
   void ensure_cand(size_t rows);
-  void ensure_embed(size_t nb);
+  void ensure_embed(EmbedScratch &e, size_t nb);
+  void free_embed(EmbedScratch &e);
+  void sync_embed_streams();
+  void flush_init();
   template <typename... A> void log(const char *fmt, A... a) const;
   void sync();
   void release_streams();
@@ -110,10 +113,20 @@ class Session {
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
   // overlap mode: the embedding phase's stream, "table published" and
-  // "embedding done" events, and whether an embedding is in flight
-  cudaStream_t estream_ = nullptr;
-  cudaEvent_t ev_pub_ = nullptr, ev_emb_ = nullptr;
-  bool emb_pending_ = false;
+  // "embedding done" events, and whether an embedding is in flight.
+  // Consecutive embedding phases alternate between two sides (stream,
+  // scratch, pinned staging), so that a phase's fuzzy set and schedule are
+  // built while the previous phase's SGD runs; "snapshot taken" marks the
+  // point after which a phase no longer reads the published table.  The
+  // insertion's embedding of its new rows runs at the start of the next
+  // phase (after the previous SGD); the insertion after it waits for that
+  // before it changes any working list.
+  cudaStream_t estream_ = nullptr, estream_alt_ = nullptr;
+  cudaEvent_t ev_pub_ = nullptr, ev_emb_ = nullptr, ev_snap_ = nullptr, ev_init_ = nullptr;
+  cudaEvent_t ev_hpin_ = nullptr, ev_hpin_alt_ = nullptr;  // each side's batch upload
+  bool emb_pending_ = false, snap_pending_ = false, init_wait_ = false;
+  bool defer_init_ = false, init_pending_ = false;
+  int init_row0_ = 0, init_nb_ = 0, init_n_ = 0;
   // ingest ring: host-to-device row transfers on their own stream, pageable
   // rows staged through two pinned slots
   static constexpr int kRingSlots = 2;
@@ -127,7 +140,7 @@ class Session {
   int ring_next_ = 0;
   DevState st_;
   UpdScratch us_;
-  EmbedScratch es_;
+  EmbedScratch es_, es_alt_;
   std::vector<void *> allocs_;
   size_t fixed_bytes_ = 0;
 
@@ -143,6 +156,8 @@ class Session {
   uint32_t *h_pin_ = nullptr;      // pinned staging (n_cap + 16 words)
   uint32_t *h_emb_pin_ = nullptr;  // the embedding phase's pinned staging
   int *es_cnt_ = nullptr;          // the embedding phase's compaction counter
+  uint32_t *h_emb_pin_alt_ = nullptr;  // the other side's (overlap mode)
+  int *es_cnt_alt_ = nullptr;
 
   size_t n_inserted_ = 0;
   size_t ins_head_ = 0;      // insertion queue = [ins_head_, n_inserted_)

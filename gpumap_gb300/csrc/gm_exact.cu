@@ -47,7 +47,13 @@ constexpr int kStages = 2;
 constexpr int kABytes = kTM * kTK * 2;         // 16 KB
 constexpr int kBBytes = kTN * kTK * 2;         // 32 KB
 constexpr int kStageBytes = 2 * kABytes + 2 * kBBytes; // 96 KB
-constexpr int kExactThreads = 192;             // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+// Warp 0 TMA, warp 1 MMA, then the epilogue: one warp group (four warps, one
+// per 32-row quarter of the tile) per column share of the tile.  The heap
+// pass keeps one group (its per-row heaps cannot be shared); the others run
+// four, each on 64 of the tile's 256 columns, so that every scheduler has
+// four epilogue warps to hide their latencies with.
+__host__ __device__ constexpr int exact_groups(int pass) { return pass == 1 ? 1 : 4; }
+__host__ __device__ constexpr int exact_threads(int pass) { return 64 + 128 * exact_groups(pass); }
 constexpr int kTmemCols = 512;                 // two 128 x 256 FP32 accumulators
 constexpr uint32_t kWaitLimit = 1u << 24;      // bounded mbarrier waits
 // epilogue column buffer: the 256 columns' squared norms, bound factors and
@@ -274,7 +280,7 @@ struct TileScreen {
 // be among m's 32 smallest.  With kKeepD the tile is also written to D (ldD
 // columns per row), for tests.
 template <int kPass, bool kKeepD>
-__global__ void __launch_bounds__(kExactThreads, 1)
+__global__ void __launch_bounds__(exact_threads(kPass), 1)
     k_exact_dist(const __grid_constant__ CUtensorMap tm_a, const __grid_constant__ CUtensorMap tm_b,
                  int arow0, int nb, int n, int kchunks, int dh, const float *norms,
                  const float *snorms, TileScreen sc, float *D, long ldD, unsigned *err) {
@@ -292,6 +298,9 @@ __global__ void __launch_bounds__(kExactThreads, 1)
   float *epi = (float *)(base + (size_t)kStages * kStageBytes + 256);
   float *heaps = (float *)((unsigned char *)epi + kEpiBytes);
 
+  constexpr int kGroups = exact_groups(kPass);
+  constexpr int kEpi = 128 * kGroups;    // epilogue threads
+  constexpr int kGroupCols = kTN / kGroups;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int mt = blockIdx.y;
   const int m0 = mt * kTM;  // batch-local first row of this tile
@@ -303,7 +312,7 @@ __global__ void __launch_bounds__(kExactThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tmem_full[b], 1);
-      mbar_init(&tmem_empty[b], 128);
+      mbar_init(&tmem_empty[b], kEpi);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -389,17 +398,20 @@ __global__ void __launch_bounds__(kExactThreads, 1)
     __syncwarp();
   } else {
     // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (tile rows), one row
-    // per thread, 32 columns per tcgen05.ld.  The four warps load a tile's
-    // column data (squared norms, bound factors, list bars) once, one tile
-    // ahead, into a double-buffered shared array that every lane reads by
-    // broadcast; each tile begins with a barrier of the 128 epilogue threads
-    // (named barrier 1), executed the same number of times by every warp.
+    // per thread, 32 columns per tcgen05.ld; warp group g = (w - 2) / 4
+    // takes columns [g * kGroupCols, +kGroupCols) of each tile.  The
+    // epilogue threads load a tile's column data (squared norms, bound
+    // factors, list bars) once, one tile ahead, into a double-buffered shared
+    // array that every lane reads by broadcast; each tile begins with a
+    // barrier of the epilogue threads (named barrier 1), executed the same
+    // number of times by every warp.
     const int quarter = warp & 3;
+    const int group = (warp - 2) >> 2;
     const int r = quarter * 32 + lane;
     const int m = m0 + r;
     const bool live = m < nb;
     const int row = arow0 + m;
-    const int et = threadIdx.x - 64;  // 0..127 over the epilogue warps
+    const int et = threadIdx.x - 64;  // 0..kEpi-1 over the epilogue warps
     const float nm = live ? norms[row] : 0.0f;
     const float sm = live ? snorms[row] : 0.0f;
     const float inf = __int_as_float(0x7f800000);
@@ -409,20 +421,26 @@ __global__ void __launch_bounds__(kExactThreads, 1)
     const float t_row = (kPass == 2 && live) ? sc.row_t[m] : inf;
     const float seed = ((kPass == 1 || kPass == 3) && live && sc.seed) ? sc.seed[m] : inf;
     int *cand_m = sc.cand + (long)m * sc.cand_ld;
-    // pass 3: this thread's segment of stored columns (row m, this CTA)
+    // pass 3: the segment of stored columns of (row m, this CTA), filled by
+    // the row's threads of every group through a shared-memory counter
+    // (in the heap space, which pass 3 does not use)
     const size_t seg = ((size_t)m * gridDim.x + blockIdx.x) * (size_t)sc.pre_cap;
-    int pcnt = 0;
+    int *scnt = reinterpret_cast<int *>(heaps);
+    if (kPass == 3 && group == 0) scnt[r] = 0;
     const bool col_test = kPass == 3 || (kPass == 1 && sc.col_test);
-    // this thread's two columns of a tile: et and et + 128
-    float cv[6];
+    // this thread's columns of a tile: et, et + kEpi, ...
+    constexpr int kColsPer = (kTN + kEpi - 1) / kEpi;
+    float cv[3 * kColsPer];
     auto load_cols = [&](int t) {
       const int c0 = t * sc.tile_stride * kTN;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int j = c0 + et + h * 128;
-        cv[3 * h] = j < n ? norms[j] : 0.0f;
-        cv[3 * h + 1] = j < n ? snorms[j] : 0.0f;
-        cv[3 * h + 2] = ((kPass == 1 || kPass == 3) && j < sc.n_exist)
+      for (int h = 0; h < kColsPer; ++h) {
+        const int jj = et + h * kEpi;
+        const int j = c0 + jj;
+        const bool in = jj < kTN && j < n;
+        cv[3 * h] = in ? norms[j] : 0.0f;
+        cv[3 * h + 1] = in ? snorms[j] : 0.0f;
+        cv[3 * h + 2] = ((kPass == 1 || kPass == 3) && jj < kTN && j < sc.n_exist)
                             ? key_dist(sc.g_key[(size_t)j * kListW + kListW - 1])
                             : -inf;
       }
@@ -434,12 +452,15 @@ __global__ void __launch_bounds__(kExactThreads, 1)
       const uint32_t b = tc & 1u;
       float *cn = epi + (size_t)b * 3 * kTN;  // norms | bound factors | list bars
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        cn[et + h * 128] = cv[3 * h];
-        cn[kTN + et + h * 128] = cv[3 * h + 1];
-        cn[2 * kTN + et + h * 128] = cv[3 * h + 2];
+      for (int h = 0; h < kColsPer; ++h) {
+        const int jj = et + h * kEpi;
+        if (jj < kTN) {
+          cn[jj] = cv[3 * h];
+          cn[kTN + jj] = cv[3 * h + 1];
+          cn[2 * kTN + jj] = cv[3 * h + 2];
+        }
       }
-      asm volatile("bar.sync 1, 128;" ::: "memory");
+      asm volatile("bar.sync 1, %0;" ::"n"(kEpi) : "memory");
       if (t + (int)gridDim.x < sc.tile_count) load_cols(t + gridDim.x);
       if (eok && !mbar_wait(&tmem_full[b], (tc >> 1) & 1)) {
         if (lane == 0) atomicOr(err, kDevErrSpin);
@@ -447,7 +468,7 @@ __global__ void __launch_bounds__(kExactThreads, 1)
       }
       if (!eok) continue;
       tc_fence_after();
-      for (int c = 0; c < kTN; c += 32) {
+      for (int c = group * kGroupCols; c < (group + 1) * kGroupCols; c += 32) {
         uint32_t v[32];
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + b * (uint32_t)kTN + (uint32_t)c, v);
         const int col0 = t * sc.tile_stride * kTN + c;
@@ -469,11 +490,11 @@ __global__ void __launch_bounds__(kExactThreads, 1)
           if (kPass == 3 && other) {
             const float lb = __fsub_rd(dv, bnd);
             if (lb <= seed) {
-              if (pcnt < sc.pre_cap) {
-                sc.pre[seg + pcnt] = ((unsigned long long)__float_as_uint(lb) << 32) | (unsigned)j;
-                sc.pre_ub[seg + pcnt] = fmaxf(__fadd_ru(dv, bnd), 0.0f);
+              const int q = atomicAdd(&scnt[r], 1);
+              if (q < sc.pre_cap) {
+                sc.pre[seg + q] = ((unsigned long long)__float_as_uint(lb) << 32) | (unsigned)j;
+                sc.pre_ub[seg + q] = fmaxf(__fadd_ru(dv, bnd), 0.0f);
               }
-              ++pcnt;
             }
           }
           if (col_test) {
@@ -508,9 +529,14 @@ __global__ void __launch_bounds__(kExactThreads, 1)
       float *out = sc.heaps + ((size_t)m * gridDim.x + blockIdx.x) * kListTop;
       for (int i = 0; i < kListTop; ++i) out[i] = i < hcnt ? heap[i * kTM] : inf;
     }
-    if (kPass == 3 && live) {
-      sc.pre_cnt[(size_t)m * gridDim.x + blockIdx.x] = min(pcnt, sc.pre_cap);
-      if (pcnt > sc.pre_cap) atomicOr(sc.pre_over, 1);
+    if (kPass == 3) {
+      // every group's stores to the row's counter are done
+      asm volatile("bar.sync 1, %0;" ::"n"(kEpi) : "memory");
+      if (group == 0 && live) {
+        const int pcnt = scnt[r];
+        sc.pre_cnt[(size_t)m * gridDim.x + blockIdx.x] = min(pcnt, sc.pre_cap);
+        if (pcnt > sc.pre_cap) atomicOr(sc.pre_over, 1);
+      }
     }
   }
   tc_fence_before();
@@ -998,7 +1024,7 @@ static void launch_tile(const DevState &st, const ExactMaps &maps, int dh, int r
   sc.g_key = st.g_key;
   sc.n_exist = row0;
   sc.coef = exact_bound_coef(st.d, dh);
-  k_exact_dist<kPass, kKeepD><<<dim3(gx, m_tiles), kExactThreads, kExactSmem, s>>>(
+  k_exact_dist<kPass, kKeepD><<<dim3(gx, m_tiles), exact_threads(kPass), kExactSmem, s>>>(
       ta, tb, row0 + blk0, nrows, n, dh / kTK, dh, st.norms, st.snorms, sc, x.D, ldD, st.err);
   note_launch();
 }

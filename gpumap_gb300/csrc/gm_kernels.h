@@ -189,6 +189,10 @@ struct EmbedScratch {
   int *ipartial = nullptr;
   int *tmp = nullptr;       // scan / compaction scratch (n_cap items)
   int *tmp2 = nullptr;      // scan / compaction scratch (cap_coo items)
+  // overlap mode: the published table as the phase's fuzzy set saw it, for
+  // its reposition step (the next cycle may publish meanwhile)
+  uint32_t *pub_idx_snap = nullptr;
+  float *pub_dist_snap = nullptr;
   size_t cap_coo = 0;
   size_t cap_partial = 0;
 };

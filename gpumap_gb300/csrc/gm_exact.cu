@@ -57,8 +57,9 @@ __host__ __device__ constexpr int exact_threads(int pass) { return 64 + 128 * ex
 constexpr int kTmemCols = 512;                 // two 128 x 256 FP32 accumulators
 constexpr uint32_t kWaitLimit = 1u << 24;      // bounded mbarrier waits
 // epilogue column buffer: the 256 columns' squared norms, bound factors and
-// list bars of a tile, double buffered (two tiles)
-constexpr size_t kEpiBytes = (size_t)2 * 3 * kTN * sizeof(float);
+// list bars of a tile, double buffered (two tiles), then per buffer eight
+// per-warp maxima of the norms and bound factors (float bits: both >= 0)
+constexpr size_t kEpiBytes = (size_t)2 * 3 * kTN * sizeof(float) + (size_t)2 * 2 * 8 * sizeof(float);
 constexpr int kListTop = 32;                   // list width the screen keeps exact
 constexpr size_t kHeapBytes = (size_t)kListTop * kTM * sizeof(float);
 constexpr size_t kExactSmem = (size_t)kStages * kStageBytes + 1024 + 256 + kEpiBytes + kHeapBytes;
@@ -301,6 +302,9 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
   constexpr int kGroups = exact_groups(kPass);
   constexpr int kEpi = 128 * kGroups;    // epilogue threads
   constexpr int kGroupCols = kTN / kGroups;
+  // warps whose columns feed the per-warp maxima, and how many per group
+  constexpr int kSlots = (kTN / ((kTN + kEpi - 1) / kEpi)) / 32 < 8 ? (kTN / ((kTN + kEpi - 1) / kEpi)) / 32 : 8;
+  constexpr int kSlotsPerGroup = kSlots / kGroups > 0 ? kSlots / kGroups : 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int mt = blockIdx.y;
   const int m0 = mt * kTM;  // batch-local first row of this tile
@@ -451,16 +455,44 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
     for (int t = blockIdx.x; t < sc.tile_count; t += gridDim.x, ++tc) {
       const uint32_t b = tc & 1u;
       float *cn = epi + (size_t)b * 3 * kTN;  // norms | bound factors | list bars
+      unsigned *mx = reinterpret_cast<unsigned *>(epi + 2 * 3 * kTN) + b * 2 * 8;
+      {
+        unsigned mn = 0, ms = 0;
 #pragma unroll
-      for (int h = 0; h < kColsPer; ++h) {
-        const int jj = et + h * kEpi;
-        if (jj < kTN) {
-          cn[jj] = cv[3 * h];
-          cn[kTN + jj] = cv[3 * h + 1];
-          cn[2 * kTN + jj] = cv[3 * h + 2];
+        for (int h = 0; h < kColsPer; ++h) {
+          const int jj = et + h * kEpi;
+          if (jj < kTN) {
+            cn[jj] = cv[3 * h];
+            cn[kTN + jj] = cv[3 * h + 1];
+            cn[2 * kTN + jj] = cv[3 * h + 2];
+            mn = max(mn, __float_as_uint(cv[3 * h]));
+            ms = max(ms, __float_as_uint(cv[3 * h + 1]));
+          }
+        }
+        const int ew = et >> 5;
+        if (ew < kSlots) {
+          mn = __reduce_max_sync(0xffffffffu, mn);
+          ms = __reduce_max_sync(0xffffffffu, ms);
+          if (lane == 0) {
+            mx[ew] = mn;
+            mx[8 + ew] = ms;
+          }
         }
       }
       asm volatile("bar.sync 1, %0;" ::"n"(kEpi) : "memory");
+      // the largest pair bound of the row over this group's columns
+      // (pair_bound is nondecreasing in the column's norm and factor)
+      float bmax;
+      {
+        unsigned mn = 0, ms = 0;
+#pragma unroll
+        for (int q = 0; q < kSlotsPerGroup; ++q) {
+          const int sl = group * kSlotsPerGroup + q;
+          mn = max(mn, mx[sl]);
+          ms = max(ms, mx[8 + sl]);
+        }
+        bmax = pair_bound(sc.coef, sm, __uint_as_float(ms), nm, __uint_as_float(mn));
+      }
       if (t + (int)gridDim.x < sc.tile_count) load_cols(t + gridDim.x);
       if (eok && !mbar_wait(&tmem_full[b], (tc >> 1) & 1)) {
         if (lane == 0) atomicOr(err, kDevErrSpin);
@@ -472,17 +504,30 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
         uint32_t v[32];
         tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + b * (uint32_t)kTN + (uint32_t)c, v);
         const int col0 = t * sc.tile_stride * kTN + c;
-        float cmin = inf;  // pass 0: this chunk's smallest upper bound
+        float cmin = inf;     // pass 0: this chunk's smallest D over other columns
+        unsigned hmask = 0;   // column test: this chunk's hit columns (bit i)
+        // passes 2 and 3: D - B of every column of the group is at least
+        // RD(D - bmax); when that exceeds the row's limit and the column's
+        // list bar in every lane, no test can pass for the column
+        const float lim = kPass == 3 ? seed : t_row;
 #pragma unroll 4
         for (int i = 0; i < 32; ++i) {
           const float nj = cn[c + i];
-          const float sj = cn[kTN + c + i];
           const int j = col0 + i;
           const float dv = __fsub_rn(__fadd_rn(nm, nj), __fmul_rn(2.0f, __uint_as_float(v[i])));
           if (kKeepD && live && j < n) D[(long)m * ldD + j] = dv;
-          const float bnd = pair_bound(sc.coef, sm, sj, nm, nj);
           const bool other = live && j < n && j != row;
-          if (kPass == 0 && other) cmin = fminf(cmin, fmaxf(__fadd_ru(dv, bnd), 0.0f));
+          if (kPass == 0) {
+            if (other) cmin = fminf(cmin, dv);
+            continue;
+          }
+          const float wj = (kPass == 1 || kPass == 3) ? cn[2 * kTN + c + i] : -inf;
+          if (kPass == 2 || kPass == 3) {
+            const float lbq = __fsub_rd(dv, bmax);
+            if (!__any_sync(0xffffffffu, lbq <= fmaxf(lim, wj))) continue;
+          }
+          const float sj = cn[kTN + c + i];
+          const float bnd = pair_bound(sc.coef, sm, sj, nm, nj);
           if (kPass == 1 && other) {
             const float ub = fmaxf(__fadd_ru(dv, bnd), 0.0f);
             if (ub < t_loc && ub <= seed) t_loc = heap_push(heap, hcnt, ub);
@@ -498,29 +543,43 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
             }
           }
           if (col_test) {
-            const float wj = cn[2 * kTN + c + i];
-            const bool hit = live && j < sc.n_exist && __fsub_rd(dv, bnd) <= wj;
-            const unsigned bal = __ballot_sync(0xffffffffu, hit);
-            if (bal) {
-              const int leader = __ffs(bal) - 1;
-              int q0 = 0;
-              if (lane == leader) q0 = atomicAdd(sc.pool_counter, __popc(bal));
-              q0 = __shfl_sync(0xffffffffu, q0, leader);
-              if (hit) {
-                const long q = (long)q0 + __popc(bal & ((1u << lane) - 1u));
-                if (q < sc.pool_cap) {
-                  sc.pool_j[q] = j;
-                  sc.pool_m[q] = m;
-                } else {
-                  atomicOr(err, kDevErrOverflow);
-                }
-              }
-            }
-          } else if (kPass == 2 && live && j < n && j != row && __fsub_rd(dv, bnd) <= t_row) {
+            if (live && j < sc.n_exist && __fsub_rd(dv, bnd) <= wj) hmask |= 1u << i;
+          } else if (kPass == 2 && other && __fsub_rd(dv, bnd) <= t_row) {
             cand_m[atomicAdd(&sc.row_cnt[m], 1)] = j;
           }
         }
-        if (kPass == 0 && live) sc.mins[(size_t)m * sc.mins_ld + t * (kTN / 32) + c / 32] = cmin;
+        if (kPass == 0 && live)
+          sc.mins[(size_t)m * sc.mins_ld + t * (kTN / 32) + c / 32] =
+              cmin == inf ? inf : fmaxf(__fadd_ru(cmin, bmax), 0.0f);
+        if (col_test) {
+          // the chunk's (existing row j, batch row m) pairs: one pool
+          // reservation per warp, lanes in order
+          const int cnt = __popc(hmask);
+          int incl = cnt;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const int total = __shfl_sync(0xffffffffu, incl, 31);
+          if (total) {
+            int base = 0;
+            if (lane == 31) base = atomicAdd(sc.pool_counter, total);
+            base = __shfl_sync(0xffffffffu, base, 31);
+            long q = (long)base + incl - cnt;
+            while (hmask) {
+              const int i = __ffs(hmask) - 1;
+              hmask &= hmask - 1;
+              if (q < sc.pool_cap) {
+                sc.pool_j[q] = col0 + i;
+                sc.pool_m[q] = m;
+              } else {
+                atomicOr(err, kDevErrOverflow);
+              }
+              ++q;
+            }
+          }
+        }
       }
       tc_fence_before();
       mbar_arrive(&tmem_empty[b]);

@@ -19,10 +19,12 @@ of them is used here.  Instead:
   baseline/_ref`` would have produced.  One object is added to the module:
   ``zeroed_new.cpp``, a zero-filling operator new with hidden visibility,
   which makes an uninitialised read in the reference's Bloom filter
-  deterministic (the file says why).  It also compiles the test driver
-  ``oracle/refbuild/ref_fuzzy_driver.cu`` (the reference's own fuzzy-set and
-  edge-scheduling functions on a k-NN table read from a file) into
-  ``baseline/_ref/bin/ref_fuzzy_driver``.
+  deterministic (the file says why).  It also compiles two test drivers
+  into ``baseline/_ref/bin``: ``ref_fuzzy_driver`` (the reference's own
+  fuzzy-set and edge-scheduling functions on a k-NN table read from a file,
+  oracle/refbuild/ref_fuzzy_driver.cu) and ``ref_embed_driver`` (its whole
+  embedding step, SGD included, on a table and an initial embedding,
+  oracle/refbuild/ref_embed_driver.cu).
 
 ``reference_available()`` says whether the built module is present.
 """
@@ -89,6 +91,10 @@ def fuzzy_driver_path() -> Path:
     return BIN / "ref_fuzzy_driver"
 
 
+def embed_driver_path() -> Path:
+    return BIN / "ref_embed_driver"
+
+
 def reference_available() -> bool:
     return core_path().exists()
 
@@ -115,6 +121,7 @@ def build(verbose: bool = False) -> Path | None:
         return None
     out = core_path()
     deps = sorted(cpp.rglob("*.cu*")) + sorted(SHIM.rglob("*.h*")) + [HERE / "ref_fuzzy_driver.cu",
+                                                                      HERE / "ref_embed_driver.cu",
                                                                       HERE / "zeroed_new.cpp",
                                                                       HERE / "zeroed_new.map"]
     OBJ.mkdir(parents=True, exist_ok=True)
@@ -129,7 +136,7 @@ def build(verbose: bool = False) -> Path | None:
                     dst.unlink()
                 shutil.copy2(f, dst)
                 dst.chmod(dst.stat().st_mode | 0o200)
-    if _newer(out, deps) and _newer(fuzzy_driver_path(), deps):
+    if _newer(out, deps) and _newer(fuzzy_driver_path(), deps) and _newer(embed_driver_path(), deps):
         return out
     nvcc = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
     if not os.path.exists(nvcc):
@@ -143,8 +150,9 @@ def build(verbose: bool = False) -> Path | None:
     cmds.append([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-c",
                  str(HERE / "zeroed_new.cpp"), "-o", str(OBJ / "zeroed_new.o")])
     BIN.mkdir(parents=True, exist_ok=True)
-    cmds.append([nvcc, *ARCH, *FLAGS, f"-I{SHIM}", f"-I{cpp / 'include'}", f"-I{cpp / 'src'}",
-                 str(HERE / "ref_fuzzy_driver.cu"), "-o", str(fuzzy_driver_path())])
+    for drv, path in (("ref_fuzzy_driver.cu", fuzzy_driver_path()), ("ref_embed_driver.cu", embed_driver_path())):
+        cmds.append([nvcc, *ARCH, *FLAGS, f"-I{SHIM}", f"-I{cpp / 'include'}", f"-I{cpp / 'src'}",
+                     str(HERE / drv), "-o", str(path)])
 
     def run(cmd):
         if verbose:
@@ -153,7 +161,7 @@ def build(verbose: bool = False) -> Path | None:
         if r.returncode != 0:
             raise RuntimeError(f"reference build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr[-6000:]}")
 
-    with ThreadPoolExecutor(max_workers=3) as ex:
+    with ThreadPoolExecutor(max_workers=4) as ex:
         list(ex.map(run, cmds))
     run([nvcc, *ARCH, "-shared", "-o", str(out), *[str(OBJ / (u.stem + ".o")) for u in units],
          str(OBJ / "zeroed_new.o"), "-Xlinker", f"--version-script={HERE / 'zeroed_new.map'}"])

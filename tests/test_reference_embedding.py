@@ -1,0 +1,111 @@
+"""The embedding step against the reference's own, on the same inputs.
+
+Both builds get one exact k-NN table (published layout: k+1 columns, squared
+L2 or 2 (1 - cos)) and one initial embedding, with every row in the batch:
+the reference's compute_fuzzy_graph and run_optimize_layout run through
+oracle/refbuild/ref_embed_driver.cu (built from its unmodified sources), this
+build's gm_op_fuzzy_schedule and gm_op_sgd through the C ABI.  Both SGDs are
+Hogwild-parallel and draw their negative samples from different generators,
+so the embeddings are compared by their quality: trustworthiness and k-NN
+preservation within 0.01 of the reference's, the tolerance the engine is held
+to.  Skipped when the reference build is absent.
+"""
+import ctypes as C
+import subprocess
+
+import numpy as np
+import pytest
+
+from gpumap_gb300.datasets import gaussian_mixture
+from oracle.knn import exact_knn, trustworthiness
+
+pytestmark = pytest.mark.gpu
+
+A, B = 1.5769434602697652, 0.8950608778515733  # find_ab_params(1.0, 0.1)
+
+
+def _driver():
+    from oracle.refbuild import build_ref
+
+    path = build_ref.embed_driver_path()
+    if not path.exists():
+        pytest.skip("reference build not installed")
+    return path
+
+
+def _knn_preservation(X, E, k, sample, metric):
+    hi, _ = exact_knn(X, k, queries=sample, metric=metric)
+    lo, _ = exact_knn(E, k, queries=sample)
+    return float(np.mean([len(set(a) & set(b)) / k for a, b in zip(hi, lo)]))
+
+
+def _table(X, k, metric):
+    n = len(X)
+    idx, dst = exact_knn(X, k, metric=metric)
+    pidx = np.zeros((n, k + 1), np.uint32)
+    pdst = np.zeros((n, k + 1), np.float32)
+    pidx[:, :k] = idx
+    pdst[:, :k] = dst
+    return pidx, pdst
+
+
+def _reference(tmp_path, pidx, pdst, emb0, k, euclid, n_epochs, nsr):
+    n = len(emb0)
+    fin, fout = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(fin, "wb") as f:
+        np.array([n, k, euclid, n_epochs, nsr], np.int32).tofile(f)
+        np.array([1.0, A, B], np.float32).tofile(f)
+        pidx.tofile(f)
+        pdst.tofile(f)
+        emb0.astype(np.float32).tofile(f)
+    subprocess.run([str(_driver()), str(fin), str(fout)], check=True, capture_output=True)
+    return np.fromfile(fout, np.float32).reshape(n, 2)
+
+
+def _ours(native, pidx, pdst, emb0, k, euclid, n_epochs, nsr):
+    import torch
+
+    n = len(emb0)
+    dev = torch.device("cuda:0")
+    t_idx = torch.from_numpy(pidx.view(np.int32)).to(dev)
+    t_dst = torch.from_numpy(pdst).to(dev)
+    batch = torch.arange(n, dtype=torch.int32, device=dev)
+    cap = 2 * n * k
+    cr, cc, tr, tc = (torch.zeros(cap, dtype=torch.int32, device=dev) for _ in range(4))
+    cv, te = torch.zeros(cap, device=dev), torch.zeros(cap, device=dev)
+    sg, rh = torch.zeros(n, device=dev), torch.zeros(n, device=dev)
+    counts = (C.c_int64 * 4)()
+    scal = (C.c_float * 3)()
+    lib = native.load()
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    native.check(lib.gm_op_fuzzy_schedule(
+        t_idx.data_ptr(), t_dst.data_ptr(), n, k, euclid, batch.data_ptr(), n, n_epochs, 1.0,
+        cr.data_ptr(), cc.data_ptr(), cv.data_ptr(), tr.data_ptr(), tc.data_ptr(), te.data_ptr(),
+        sg.data_ptr(), rh.data_ptr(), counts, scal, stream))
+    emb = torch.from_numpy(emb0.astype(np.float32).copy()).to(dev)
+    native.check(lib.gm_op_sgd(emb.data_ptr(), n, tr.data_ptr(), tc.data_ptr(), te.data_ptr(), counts[2],
+                               scal[2], 1.0, 1.0, A, B, n_epochs, nsr, 42, stream))
+    torch.cuda.synchronize()
+    return emb.cpu().numpy()
+
+
+@pytest.mark.parametrize("metric,n,d,k,seed", [("euclidean", 4000, 32, 15, 31), ("cosine", 3000, 48, 30, 32)])
+def test_embedding_quality_matches_reference(native, tmp_path, metric, n, d, k, seed):
+    X, _ = gaussian_mixture(n, d, seed=seed)
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    euclid = int(metric == "euclidean")
+    pidx, pdst = _table(X, k, metric)
+    emb0 = np.random.default_rng(seed).uniform(-10.0, 10.0, size=(n, 2)).astype(np.float32)
+    e_ref = _reference(tmp_path, pidx, pdst, emb0, k, euclid, 200, 5)
+    e_our = _ours(native, pidx, pdst, emb0, k, euclid, 200, 5)
+    assert np.all(np.isfinite(e_ref)) and np.all(np.isfinite(e_our))
+    sample = np.arange(0, n, 2)
+    q = 15
+    # quality in the metric's own geometry (cosine: unit rows)
+    Xq = X / np.linalg.norm(X, axis=1, keepdims=True) if metric == "cosine" else X
+    t_ref, t_our = trustworthiness(Xq, e_ref, q, sample=sample), trustworthiness(Xq, e_our, q, sample=sample)
+    p_ref = _knn_preservation(Xq, e_ref, q, sample, "euclidean")
+    p_our = _knn_preservation(Xq, e_our, q, sample, "euclidean")
+    assert abs(t_our - t_ref) <= 0.01, (t_our, t_ref)
+    assert abs(p_our - p_ref) <= 0.01, (p_our, p_ref)
+    assert t_ref > 0.8, t_ref  # the reference itself embedded the clusters

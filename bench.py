@@ -371,15 +371,19 @@ def run_target_latency(X_host, n, d, q_idx, exact, precision, overlap, target_s=
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from
 # ncu captures of the 30,000-point cut of this workload (k_exact_dist: the
-# launch of cycle 41, 20,500 columns; k_sgd_persistent: the launch of cycle
-# 40).  "per" names the unit the traffic scales with, so that a capture can
-# be carried to this run's mean launch: k_exact_dist reads its B operand once
-# per launch (bytes ~ FLOPs); the SGD launch's traffic is the first touch of
-# its edge arrays (about the same per embedding call at any size, so it is
-# used as measured).
+# seed and store passes of cycle 31, 15,500 columns; k_sgd_persistent: the
+# launch of cycle 40).  "per" names the unit the traffic scales with, so that
+# a capture can be carried to this run's mean launch: the tile passes read
+# their column operand once per block (bytes ~ FLOPs); the SGD launch's
+# traffic is the first touch of its edge arrays (about the same per
+# embedding call at any size, so it is used as measured).
 NCU_TRAFFIC = {
-    "k_exact_dist": {"bytes": 69587968 + 5130496, "per": "flop", "units": 6 * 500 * 20500 * 832},
-    "k_sgd_persistent": {"bytes": 864512 + 79104, "per": "launch", "units": 1},
+    # one insertion block of 500 rows against 15,500 columns (dh 832): the
+    # seed pass plus the store pass, DRAM read + write; scaled by FLOPs
+    "k_exact_dist": {"bytes": (15401728 + 512) + (54068736 + 2715904), "per": "flop",
+                     "units": 6 * 500 * 15500 * 832},
+    # one embedding call (1,000 rows, ~26.7k edges, 200 epochs)
+    "k_sgd_persistent": {"bytes": 870400 + 75008, "per": "launch", "units": 1},
 }
 
 

@@ -378,14 +378,12 @@ int gm_op_sgd(float *emb, int64_t n, const int32_t *head, const int32_t *tail,
   cudaStream_t s = (cudaStream_t)stream;
   return guarded([&] {
     if (nnz == 0 || n_epochs == 0) return;
-    void *ns = nullptr, *nn = nullptr, *sc = nullptr, *pm = nullptr;
+    void *ns = nullptr, *nn = nullptr, *sc = nullptr;
     if (cudaMalloc(&ns, (size_t)nnz * 4) != cudaSuccess || cudaMalloc(&nn, (size_t)nnz * 4) != cudaSuccess ||
-        cudaMalloc(&pm, (size_t)nnz * 4) != cudaSuccess ||
-        cudaMalloc(&sc, 128 + gm::kSgdEpsBins * 4) != cudaSuccess) {
+        cudaMalloc(&sc, 128) != cudaSuccess) {
       cudaGetLastError();
       cudaFree(ns);
       cudaFree(nn);
-      cudaFree(pm);
       cudaFree(sc);
       throw gm::Error(GM_ERR_OOM, "cudaMalloc");
     }
@@ -404,15 +402,14 @@ int gm_op_sgd(float *emb, int64_t n, const int32_t *head, const int32_t *tail,
     int *isc = (int *)sc;
     const cudaError_t le = gm::launch_sgd_call(
         emb, head, tail, eps, (float *)ns, (float *)nn, isc, (const float *)((char *)sc + 64),
-        alpha0, gamma, a, b, n_epochs, neg_rate, seed, (int *)pm, (int *)((char *)sc + 128),
-        (unsigned *)(isc + gm::kIscalBarrier), (unsigned *)(isc + 10), dev, s);
+        alpha0, gamma, a, b, n_epochs, neg_rate, seed, (unsigned *)(isc + gm::kIscalBarrier),
+        (unsigned *)(isc + 10), dev, s);
     unsigned dev_err = 0;
     if (le == cudaSuccess) cudaMemcpyAsync(&dev_err, isc + 10, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
     const cudaError_t err = le != cudaSuccess ? le : cudaStreamSynchronize(s);
     if (le != cudaSuccess) cudaGetLastError();
     cudaFree(ns);
     cudaFree(nn);
-    cudaFree(pm);
     cudaFree(sc);
     if (err != cudaSuccess) throw gm::Error(GM_ERR_CUDA, cudaGetErrorString(err));
     if (dev_err) throw gm::Error(GM_ERR_DEVICE, "SGD grid barrier wait ran out");

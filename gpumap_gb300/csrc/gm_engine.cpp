@@ -953,9 +953,8 @@ void Session::run_sgd(cudaStream_t s) {
   const int max_ctas = p_.overlap ? std::max(1, sms_ / 2) : 0;
   ck(launch_sgd_call(st_.emb, es_.t_row, es_.flag_tail, es_.t_val, es_.next_s, es_.next_n,
                      es_.iscal, es_.fscal, p_.alpha, 1.0f, p_.a, p_.b, (int)p_.max_epoch,
-                     (int)p_.negative_sample_rate, 42ull, es_.t_col, es_.ipartial,
-                     (unsigned *)(es_.iscal + kIscalBarrier), st_.err, device_, s, st_.stat,
-                     max_ctas),
+                     (int)p_.negative_sample_rate, 42ull, (unsigned *)(es_.iscal + kIscalBarrier),
+                     st_.err, device_, s, st_.stat, max_ctas),
      "SGD launch");
 }
 

@@ -222,24 +222,21 @@ void launch_sgd(float *emb, const int *head, const int *tail, const float *eps,
 // All n_epochs epochs in one cooperative launch (one CTA of 512 threads per
 // SM, at most max_ctas CTAs when max_ctas > 0) with a bounded grid barrier
 // between epochs; bar: 1 device word,
-// cleared here; a barrier timeout sets kDevErrSpin in *err.  perm (nnz ints)
-// and bins (kSgdEpsBins ints), when given, receive the edges grouped by
-// sampling period (threads of a warp then tend to be active together).
-constexpr int kSgdEpsBins = 256;
+// cleared here; a barrier timeout sets kDevErrSpin in *err.  Edges run in
+// the schedule's order, one per thread slot.
 cudaError_t launch_sgd_persistent(float *emb, const int *head, const int *tail,
                                   const float *eps, float *next_s, float *next_n,
                                   const int *iscal, const float *fscal, float alpha0,
                                   float gamma, float a, float b, int n_epochs, int neg_rate,
-                                  uint64_t seed, int *perm, int *bins, unsigned *bar,
-                                  unsigned *err, int device, cudaStream_t s,
-                                  unsigned long long *stat = nullptr, int max_ctas = 0);
+                                  uint64_t seed, unsigned *bar, unsigned *err, int device,
+                                  cudaStream_t s, unsigned long long *stat = nullptr,
+                                  int max_ctas = 0);
 // One embedding call's SGD (all epochs): launch_sgd_persistent.
 cudaError_t launch_sgd_call(float *emb, const int *head, const int *tail, const float *eps,
                             float *next_s, float *next_n, const int *iscal, const float *fscal,
                             float alpha0, float gamma, float a, float b, int n_epochs, int neg_rate,
-                            uint64_t seed, int *perm, int *bins, unsigned *bar, unsigned *err,
-                            int device, cudaStream_t s, unsigned long long *stat = nullptr,
-                            int max_ctas = 0);
+                            uint64_t seed, unsigned *bar, unsigned *err, int device,
+                            cudaStream_t s, unsigned long long *stat = nullptr, int max_ctas = 0);
 void launch_set_int(int *p, int v, cudaStream_t s);
 constexpr int kIscalN = 4;
 constexpr int kIscalBarrier = 8;  // iscal[8..9]: SGD grid-barrier words

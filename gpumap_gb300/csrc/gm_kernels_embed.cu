@@ -396,13 +396,11 @@ GM_D int sgd_n_neg(float fe, float nn, float ep_neg) {
   return (int)__fdiv_rn(__fsub_rn(fe, nn), ep_neg);
 }
 
-// One edge of one epoch.  The positions of the head, the tail and of the
+// One edge of one epoch.  The head and tail positions are read first; the
 // first kNegAhead negative samples (rows from this edge's Philox stream,
 // blocks 0 and 1, words in order, computed directly into registers) are
-// fetched together, ahead of the sequential updates.  A sample that is this
-// edge's own tail is advanced by this thread's tail update, which in
-// sequential order precedes the read.  powf(d2, b - 1) and powf(d2, b) share
-// one log.
+// fetched together after the attraction and the tail update, ahead of the
+// sequential repulsions.  powf(d2, b - 1) and powf(d2, b) share one log.
 GM_D void sgd_edge(float *emb, int row, int j, int kk, float ep, float &ns, float &nn, int n,
                    uint64_t M, float rounding, float alpha, float fe, float gamma, float a,
                    float b, float nsr_inv, uint64_t seed, unsigned &my_edges, unsigned &my_negs) {
@@ -424,7 +422,6 @@ GM_D void sgd_edge(float *emb, int row, int j, int kk, float ep, float &ns, floa
     for (int p = 0; p < kNegAhead; ++p) {
       if (p < n_neg) {
         rr[p] = (int)fastmod(w[p], M, (uint32_t)n);
-        qq[p] = ld_pos(emb + (size_t)rr[p] * 2);
       }
     }
   }
@@ -448,6 +445,13 @@ GM_D void sgd_edge(float *emb, int row, int j, int kk, float ep, float &ns, floa
   // atomically, exactly as two scalar adds; rows are 8-byte aligned)
   atomicAdd(reinterpret_cast<float2 *>(op), make_float2(t0, t1));
   ns = __fadd_rn(ns, ep);
+  // the samples' positions are read after the attraction, where the
+  // reference reads them: by then the epoch's attraction updates are landing,
+  // and the repulsion must see them (read at the start of the edge, they
+  // give a measurably different layout); fetched together, one round trip
+#pragma unroll
+  for (int p = 0; p < kNegAhead; ++p)
+    if (p < n_neg) qq[p] = ld_pos(emb + (size_t)rr[p] * 2);
   if (n_neg > 0) {
     const float two_gb = __fmul_rn(__fmul_rn(2.0f, gamma), b);
     const float a4 = __fmul_rn(4.0f, alpha);
@@ -472,11 +476,7 @@ GM_D void sgd_edge(float *emb, int row, int j, int kk, float ep, float &ns, floa
     };
 #pragma unroll
     for (int p = 0; p < kNegAhead; ++p) {
-      if (p < n_neg) {
-        const bool own = rr[p] == kk;
-        negative(rr[p], own ? __fadd_rn(qq[p].x, t0) : qq[p].x,
-                 own ? __fadd_rn(qq[p].y, t1) : qq[p].y);
-      }
+      if (p < n_neg) negative(rr[p], qq[p].x, qq[p].y);
     }
     if (n_neg > kNegAhead) {
       // draws past kNegAhead: the same stream from block 2 on
@@ -589,18 +589,18 @@ __global__ void __launch_bounds__(kSgdThreads)
     k_sgd_persistent(float *emb, const int *head, const int *tail, const int *iscal,
                      const float *eps, float *next_s, float *next_n, float alpha0, int n_epochs,
                      float gamma, float a, float b, float nsr_inv, uint64_t seed,
-                     const float *fscal, const int *perm, unsigned *bar, unsigned *err,
+                     const float *fscal, unsigned *bar, unsigned *err,
                      unsigned long long *stat) {
   const int nnz = iscal[IS_NNZ2], n = iscal[IS_N];
   const uint64_t M = ~0ull / (uint64_t)max(n, 1) + 1ull;
   const float rounding = fscal[FS_ROUND];
   unsigned my_edges = 0, my_negs = 0;
-  // slot i of the grid handles edge perm[i] (edges grouped by sampling period,
-  // so that a warp's lanes tend to be active in the same epochs).  Warp-sized
-  // runs of slots are dealt round-robin over the CTAs (run w to CTA
-  // w mod gridDim.x), so the edges of each period, and the busiest ones,
-  // spread over every SM instead of filling the first few; the map from
-  // (CTA, thread) to slot is a bijection on [0, gridDim.x * blockDim.x).
+  // slot i of the grid handles edge i, in the schedule's order (a head's
+  // edges in adjacent lanes, as in the reference's one-thread-per-edge
+  // epochs).  Warp-sized runs of slots are dealt round-robin over the CTAs
+  // (run w to CTA w mod gridDim.x), so the active edges spread over every SM
+  // instead of filling the first few; the map from (CTA, thread) to slot is
+  // a bijection on [0, gridDim.x * blockDim.x).
   const int first = (((int)threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x) * 32 + ((int)threadIdx.x & 31);
   const int stride = gridDim.x * blockDim.x;
   int rrow[kRegEdges], rj[kRegEdges], rk[kRegEdges];
@@ -609,7 +609,7 @@ __global__ void __launch_bounds__(kSgdThreads)
   for (int t = 0; t < kRegEdges; ++t) {
     const int slot = first + t * stride;
     if (slot < nnz) {
-      const int row = perm ? perm[slot] : slot;
+      const int row = slot;
       rrow[t] = row;
       rj[t] = head[row], rk[t] = tail[row], rep[t] = eps[row];
       rns[t] = next_s[row], rnn[t] = next_n[row];
@@ -625,8 +625,7 @@ __global__ void __launch_bounds__(kSgdThreads)
         sgd_edge(emb, rrow[t], rj[t], rk[t], rep[t], rns[t], rnn[t], n, M, rounding, alpha, fe,
                  gamma, a, b, nsr_inv, sd, my_edges, my_negs);
     }
-    for (int slot = first + kRegEdges * stride; slot < nnz; slot += stride) {
-      const int row = perm ? perm[slot] : slot;
+    for (int row = first + kRegEdges * stride; row < nnz; row += stride) {
       float ns = next_s[row];
       if (ns > fe) continue;
       float nn = next_n[row];
@@ -645,39 +644,6 @@ __global__ void __launch_bounds__(kSgdThreads)
   for (int t = 0; t < kRegEdges; ++t)
     if (first + t * stride < nnz) next_s[rrow[t]] = rns[t], next_n[rrow[t]] = rnn[t];
   sgd_stats(my_edges, my_negs, stat);
-}
-
-// Edge grouping by sampling period: counting sort of the edges on
-// min(floor(8 * epochs_per_sample), kEpsBins - 1) into perm.
-constexpr int kEpsBins = 256;
-GM_D int eps_bin(float e) {
-  const float v = __fmul_rn(e, 8.0f);
-  return v < (float)(kEpsBins - 1) ? max((int)v, 0) : kEpsBins - 1;
-}
-__global__ void k_eps_hist(const float *eps, const int *iscal, int *bins) {
-  __shared__ int h[kEpsBins];
-  for (int i = threadIdx.x; i < kEpsBins; i += blockDim.x) h[i] = 0;
-  __syncthreads();
-  const int nnz = iscal[IS_NNZ2];
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += gridDim.x * blockDim.x)
-    atomicAdd(&h[eps_bin(eps[q])], 1);
-  __syncthreads();
-  for (int i = threadIdx.x; i < kEpsBins; i += blockDim.x)
-    if (h[i]) atomicAdd(&bins[i], h[i]);
-}
-__global__ void k_eps_scan(int *bins) {  // one block of kEpsBins threads
-  __shared__ int v[kEpsBins];
-  const int t = threadIdx.x;
-  v[t] = bins[t];
-  __syncthreads();
-  int acc = 0;
-  for (int i = 0; i < t; ++i) acc += v[i];
-  bins[t] = acc;
-}
-__global__ void k_eps_scatter(const float *eps, const int *iscal, int *bins, int *perm) {
-  const int nnz = iscal[IS_NNZ2];
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nnz; q += gridDim.x * blockDim.x)
-    perm[atomicAdd(&bins[eps_bin(eps[q])], 1)] = q;
 }
 
 __global__ void k_set_int(int *p, int v) { *p = v; }
@@ -879,9 +845,6 @@ void launch_sgd(float *emb, const int *head, const int *tail, const float *eps,
   }
 }
 
-static void group_edges(const float *eps, const int *iscal, int *perm, int *bins, int grid,
-                        cudaStream_t s);
-
 int sgd_persistent_grid(int device) {
   // per device, once (sessions on several host threads may launch at once)
   static std::mutex mu;
@@ -901,44 +864,30 @@ cudaError_t launch_sgd_persistent(float *emb, const int *head, const int *tail,
                                   const float *eps, float *next_s, float *next_n,
                                   const int *iscal, const float *fscal, float alpha0,
                                   float gamma, float a, float b, int n_epochs, int neg_rate,
-                                  uint64_t seed, int *perm, int *bins, unsigned *bar,
-                                  unsigned *err, int device, cudaStream_t s,
-                                  unsigned long long *stat, int max_ctas) {
+                                  uint64_t seed, unsigned *bar, unsigned *err, int device,
+                                  cudaStream_t s, unsigned long long *stat, int max_ctas) {
   if (n_epochs <= 0) return cudaSuccess;
   int grid = sgd_persistent_grid(device);
   if (max_ctas > 0) grid = std::min(grid, max_ctas);
   if (grid <= 0) return cudaErrorInvalidDevice;
   cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(unsigned), s);
   if (e != cudaSuccess) return e;
-  if (perm) group_edges(eps, iscal, perm, bins, grid, s);
   float nsr_inv = 1.0f / (float)neg_rate;
-  const int *cperm = perm;
   void *args[] = {&emb, &head, &tail, &iscal, &eps, &next_s, &next_n, &alpha0, &n_epochs,
-                  &gamma, &a, &b, &nsr_inv, &seed, &fscal, &cperm, &bar, &err, &stat};
+                  &gamma, &a, &b, &nsr_inv, &seed, &fscal, &bar, &err, &stat};
   e = cudaLaunchCooperativeKernel((const void *)k_sgd_persistent, dim3(grid), dim3(kSgdThreads),
                                   args, 0, s);
   note_launch();
   return e;
 }
 
-// Edge grouping (counting sort on the sampling period) into perm/bins.
-static void group_edges(const float *eps, const int *iscal, int *perm, int *bins, int grid,
-                        cudaStream_t s) {
-  cudaMemsetAsync(bins, 0, kEpsBins * sizeof(int), s);
-  k_eps_hist<<<grid, 256, 0, s>>>(eps, iscal, bins);
-  k_eps_scan<<<1, kEpsBins, 0, s>>>(bins);
-  k_eps_scatter<<<grid, 256, 0, s>>>(eps, iscal, bins, perm);
-  note_launch(3);
-}
-
 cudaError_t launch_sgd_call(float *emb, const int *head, const int *tail, const float *eps,
                             float *next_s, float *next_n, const int *iscal, const float *fscal,
                             float alpha0, float gamma, float a, float b, int n_epochs, int neg_rate,
-                            uint64_t seed, int *perm, int *bins, unsigned *bar, unsigned *err,
-                            int device, cudaStream_t s, unsigned long long *stat, int max_ctas) {
+                            uint64_t seed, unsigned *bar, unsigned *err, int device, cudaStream_t s,
+                            unsigned long long *stat, int max_ctas) {
   return launch_sgd_persistent(emb, head, tail, eps, next_s, next_n, iscal, fscal, alpha0, gamma,
-                               a, b, n_epochs, neg_rate, seed, perm, bins, bar, err, device, s,
-                               stat, max_ctas);
+                               a, b, n_epochs, neg_rate, seed, bar, err, device, s, stat, max_ctas);
 }
 
 void launch_add_noise(float *emb, int n, const int *batch, int nb, float noise_scale,

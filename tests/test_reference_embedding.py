@@ -89,7 +89,8 @@ def _ours(native, pidx, pdst, emb0, k, euclid, n_epochs, nsr):
     return emb.cpu().numpy()
 
 
-@pytest.mark.parametrize("metric,n,d,k,seed", [("euclidean", 4000, 32, 15, 31), ("cosine", 3000, 48, 30, 32)])
+@pytest.mark.parametrize("metric,n,d,k,seed", [("euclidean", 2000, 24, 15, 33), ("euclidean", 4000, 32, 15, 31),
+                                               ("cosine", 3000, 48, 30, 32)])
 def test_embedding_quality_matches_reference(native, tmp_path, metric, n, d, k, seed):
     X, _ = gaussian_mixture(n, d, seed=seed)
     X = np.ascontiguousarray(X, dtype=np.float32)

@@ -312,6 +312,28 @@ def test_exact_mode_seeded_screen_bitexact(native, oracle_mod, cap):
         assert over == 0, over
 
 
+def test_exact_mode_cosine_k30_seeded_bitexact(native, oracle_mod):
+    # the widest list (k = 30) on the cosine metric, past the seeded store
+    # pass's threshold (33+ column tiles), against the oracle's brute force
+    n, d, k = 10000, 48, 30
+    X, _ = gaussian_mixture(n, d, seed=41)
+    s = native.Session(native.default_params(n_instances=n, n_features=d, n_neighbors=k, metric=1,
+                                             max_epoch=10, device=0, precision=1))
+    o = oracle_mod.OracleSession(n, d, k=k, metric=1, max_epoch=10, precision=1)
+    c0 = 0
+    for rows in [4000, 4000, 1000, 1000]:
+        chunk = X[c0 : c0 + rows]
+        c0 += rows
+        s.append_host(chunk)
+        o.append(chunk)
+        same_result(s.run(rows, 0, 300), o.run(rows, 0, 300))
+        same_state(s, o, tag=f"cosine k30 rows {c0}")
+    same_state(s, o, embed=True, tag="cosine k30 final")
+    ei, _ = exact_knn(X, k, metric="cosine", queries=np.arange(0, n, 7))
+    idx = s.copy("pub_idx", U32).reshape(n, k + 1)[:, :k]
+    assert recall_at_k(idx[np.arange(0, n, 7)], ei) > 0.99
+
+
 # ---------------------------------------------------------------------------
 # overlap = 1: each cycle's embedding runs on its own stream beside the next
 # cycle's distance work; everything the oracle pins must be unchanged

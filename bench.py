@@ -567,7 +567,8 @@ def cosine_1m_run(native, n=1_000_000, d=128, k=30, chunk=10_000, queries=10_000
         "points_per_s": n / wall, "seconds": wall, "recall_at_30": recall(idx[q], ex),
         "phase_s": phase, "tensor_tile_ms": st.exact_ms, "screen_ms": st.exact_ms and st.screen_ms,
         "tensor_tflops": st.exact_flops / (st.exact_ms / 1e3) / 1e12 if st.exact_ms else None,
-        "sgd_ms": st.sgd_ms, "pairs_screened": int(st.exact_pairs), "pairs_rescored": int(st.exact_rescored)}
+        "sgd_ms": st.sgd_ms, "pairs_screened": int(st.exact_pairs), "pairs_rescored": int(st.exact_rescored),
+        "overflow_blocks": int(st.exact_overflow_blocks), "kernel_launches": int(st.kernel_launches)}
     del s
     m = min(fp32_rows, n)
     s, wall, phase, st = build(X_dev[:m], 0, chunk, chunk)

@@ -156,11 +156,16 @@ Session::Session(const gm_params &p) : p_(p) {
       ck(cudaMallocHost((void **)&h_emb_pin_alt_, (Nm + 64) * sizeof(uint32_t)), "cudaMallocHost");
     if (p.precision == 1) {
       // split-BF16 shadow rows (hi | lo, 2 x dh bf16 each) plus a block of
-      // candidate / pair scratch sized so that a block holds at most ~256 MB
-      // of each (at least 128 rows)
+      // candidate / pair scratch for the worst case (every column a
+      // candidate of every block row): 28 bytes per (block row, row).  The
+      // block takes up to 1,024 rows (fewer, longer launches) within an
+      // eighth of the device's memory and at most 32 GB, and at least 128
       dh_ = exact_dh((int)d);
       xh_ = dalloc(Nm * (size_t)dh_ * 4);
-      ex_block_ = (int)std::max<size_t>(128, std::min<size_t>(4096, ((size_t)256 << 20) / (Nm * 4)));
+      size_t free_b = 0, total_b = 0;
+      ck(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+      const size_t budget = std::min<size_t>(total_b / 8, (size_t)32 << 30);
+      ex_block_ = (int)std::max<size_t>(128, std::min<size_t>(1024, budget / (Nm * 28)));
       ex_block_ = ex_block_ / 128 * 128;
       // the approximate tile itself is only stored on request (tests), in
       // a buffer allocated then
@@ -329,7 +334,15 @@ void Session::drain() {
   check_device_error("embedding");
 }
 
+void Session::check_launch_error(const char *phase) {
+  // a launch the runtime refused (resources, configuration) is reported
+  // once, by the next query of the last error
+  const cudaError_t le = cudaGetLastError();
+  if (le != cudaSuccess) ck(le, (std::string(phase) + " launch").c_str());
+}
+
 void Session::check_device_error(const char *phase) {
+  check_launch_error(phase);
   unsigned e = 0;
   ck(cudaMemcpyAsync(&e, st_.err, sizeof(unsigned), cudaMemcpyDeviceToHost, stream_), "err");
   sync();
@@ -360,6 +373,7 @@ void Session::ensure_cand(size_t rows) {
 void Session::set_pre_cap(int cap) {
   drain();
   xs_.pre_cap = std::max(0, std::min(cap, pre_cap_alloc_));
+  xs_.pre_fixed = true;
 }
 
 void Session::set_keep_tile(bool on) {
@@ -612,6 +626,8 @@ gm_result Session::run(uint32_t n_ins, uint32_t n_upd, uint32_t n_emb) {
     if (!p_.overlap) {
       sync();
       check_device_error("embedding");
+    } else {
+      check_launch_error("embedding");
     }
     const auto t1 = Clock::now();
     r.embedding_time = std::chrono::duration<float>(t1 - t0).count();

@@ -95,6 +95,7 @@ class Session {
   uint32_t update(uint32_t n_ops, size_t &changed_edges);
   size_t update_round(std::vector<uint32_t> &batch, std::vector<uint32_t> &affected);
   uint32_t embed(uint32_t n_ops);
+  void check_launch_error(const char *phase);
   void check_device_error(const char *phase);
   void ensure_cand(size_t rows);
   void ensure_embed(EmbedScratch &e, size_t nb);

@@ -59,7 +59,7 @@ constexpr uint32_t kWaitLimit = 1u << 24;      // bounded mbarrier waits
 // epilogue column buffer: the 256 columns' squared norms, bound factors and
 // list bars of a tile, double buffered (two tiles), then per buffer eight
 // per-warp maxima of the norms and bound factors (float bits: both >= 0)
-constexpr size_t kEpiBytes = (size_t)2 * 3 * kTN * sizeof(float) + (size_t)2 * 2 * 8 * sizeof(float);
+constexpr size_t kEpiBytes = (size_t)2 * 3 * kTN * sizeof(float) + (size_t)2 * 2 * 16 * sizeof(float);
 constexpr int kListTop = 32;                   // list width the screen keeps exact
 constexpr size_t kHeapBytes = (size_t)kListTop * kTM * sizeof(float);
 constexpr size_t kExactSmem = (size_t)kStages * kStageBytes + 1024 + 256 + kEpiBytes + kHeapBytes;
@@ -147,18 +147,24 @@ GM_D void umma_commit(uint64_t *bar) {
 GM_D void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 GM_D void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-GM_D void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+// 16 consecutive columns of this thread's lane; the registers are valid after
+// tmem_ld_wait (which names them, so that no read of them moves above it)
+GM_D void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
         "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+GM_D void tmem_ld_wait(uint32_t (&r)[16]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                 "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+               :
+               : "memory");
 }
 
 // Batch rows to split BF16 (both halves round to nearest): shadow row =
@@ -302,9 +308,6 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
   constexpr int kGroups = exact_groups(kPass);
   constexpr int kEpi = 128 * kGroups;    // epilogue threads
   constexpr int kGroupCols = kTN / kGroups;
-  // warps whose columns feed the per-warp maxima, and how many per group
-  constexpr int kSlots = (kTN / ((kTN + kEpi - 1) / kEpi)) / 32 < 8 ? (kTN / ((kTN + kEpi - 1) / kEpi)) / 32 : 8;
-  constexpr int kSlotsPerGroup = kSlots / kGroups > 0 ? kSlots / kGroups : 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int mt = blockIdx.y;
   const int m0 = mt * kTM;  // batch-local first row of this tile
@@ -403,19 +406,21 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
   } else {
     // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (tile rows), one row
     // per thread, 32 columns per tcgen05.ld; warp group g = (w - 2) / 4
-    // takes columns [g * kGroupCols, +kGroupCols) of each tile.  The
-    // epilogue threads load a tile's column data (squared norms, bound
-    // factors, list bars) once, one tile ahead, into a double-buffered shared
-    // array that every lane reads by broadcast; each tile begins with a
-    // barrier of the epilogue threads (named barrier 1), executed the same
-    // number of times by every warp.
+    // takes columns [g * kGroupCols, +kGroupCols) of each tile.  Each group
+    // loads its columns' data (squared norms, bound factors, list bars) one
+    // tile ahead into a double-buffered shared array that its lanes read by
+    // broadcast; each tile begins with a barrier of the group's 128 threads
+    // (named barrier 1 + g), executed the same number of times by each of
+    // them, so that groups run on without waiting for one another.  Named
+    // barrier 5 spans the whole epilogue (before the first tile and, in pass
+    // 3, after the last).
     const int quarter = warp & 3;
     const int group = (warp - 2) >> 2;
     const int r = quarter * 32 + lane;
     const int m = m0 + r;
     const bool live = m < nb;
     const int row = arow0 + m;
-    const int et = threadIdx.x - 64;  // 0..kEpi-1 over the epilogue warps
+    const int gt = threadIdx.x - 64 - 128 * group;  // 0..127 within the group
     const float nm = live ? norms[row] : 0.0f;
     const float sm = live ? snorms[row] : 0.0f;
     const float inf = __int_as_float(0x7f800000);
@@ -431,20 +436,22 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
     const size_t seg = ((size_t)m * gridDim.x + blockIdx.x) * (size_t)sc.pre_cap;
     int *scnt = reinterpret_cast<int *>(heaps);
     if (kPass == 3 && group == 0) scnt[r] = 0;
+    asm volatile("bar.sync 5, %0;" ::"n"(kEpi) : "memory");
     const bool col_test = kPass == 3 || (kPass == 1 && sc.col_test);
-    // this thread's columns of a tile: et, et + kEpi, ...
-    constexpr int kColsPer = (kTN + kEpi - 1) / kEpi;
+    // this thread's columns of a tile: group * kGroupCols + gt + 128 h
+    constexpr int kColsPer = (kGroupCols + 127) / 128;
     float cv[3 * kColsPer];
     auto load_cols = [&](int t) {
       const int c0 = t * sc.tile_stride * kTN;
 #pragma unroll
       for (int h = 0; h < kColsPer; ++h) {
-        const int jj = et + h * kEpi;
+        const int gi = gt + h * 128;
+        const int jj = group * kGroupCols + gi;
         const int j = c0 + jj;
-        const bool in = jj < kTN && j < n;
+        const bool in = gi < kGroupCols && j < n;
         cv[3 * h] = in ? norms[j] : 0.0f;
         cv[3 * h + 1] = in ? snorms[j] : 0.0f;
-        cv[3 * h + 2] = ((kPass == 1 || kPass == 3) && jj < kTN && j < sc.n_exist)
+        cv[3 * h + 2] = ((kPass == 1 || kPass == 3) && gi < kGroupCols && j < sc.n_exist)
                             ? key_dist(sc.g_key[(size_t)j * kListW + kListW - 1])
                             : -inf;
       }
@@ -455,13 +462,16 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
     for (int t = blockIdx.x; t < sc.tile_count; t += gridDim.x, ++tc) {
       const uint32_t b = tc & 1u;
       float *cn = epi + (size_t)b * 3 * kTN;  // norms | bound factors | list bars
-      unsigned *mx = reinterpret_cast<unsigned *>(epi + 2 * 3 * kTN) + b * 2 * 8;
+      // per-warp maxima of the column norms and factors: slot 4 g + q for
+      // warp q of group g (0 where the warp has no columns)
+      unsigned *mx = reinterpret_cast<unsigned *>(epi + 2 * 3 * kTN) + b * 2 * 16;
       {
         unsigned mn = 0, ms = 0;
 #pragma unroll
         for (int h = 0; h < kColsPer; ++h) {
-          const int jj = et + h * kEpi;
-          if (jj < kTN) {
+          const int gi = gt + h * 128;
+          if (gi < kGroupCols) {
+            const int jj = group * kGroupCols + gi;
             cn[jj] = cv[3 * h];
             cn[kTN + jj] = cv[3 * h + 1];
             cn[2 * kTN + jj] = cv[3 * h + 2];
@@ -469,27 +479,28 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
             ms = max(ms, __float_as_uint(cv[3 * h + 1]));
           }
         }
-        const int ew = et >> 5;
-        if (ew < kSlots) {
-          mn = __reduce_max_sync(0xffffffffu, mn);
-          ms = __reduce_max_sync(0xffffffffu, ms);
-          if (lane == 0) {
-            mx[ew] = mn;
-            mx[8 + ew] = ms;
-          }
+        mn = __reduce_max_sync(0xffffffffu, mn);
+        ms = __reduce_max_sync(0xffffffffu, ms);
+        if (lane == 0) {
+          mx[4 * group + quarter] = mn;
+          mx[16 + 4 * group + quarter] = ms;
         }
       }
-      asm volatile("bar.sync 1, %0;" ::"n"(kEpi) : "memory");
+      switch (group) {  // the barrier id is an immediate
+        case 0: asm volatile("bar.sync 1, 128;" ::: "memory"); break;
+        case 1: asm volatile("bar.sync 2, 128;" ::: "memory"); break;
+        case 2: asm volatile("bar.sync 3, 128;" ::: "memory"); break;
+        default: asm volatile("bar.sync 4, 128;" ::: "memory"); break;
+      }
       // the largest pair bound of the row over this group's columns
       // (pair_bound is nondecreasing in the column's norm and factor)
       float bmax;
       {
         unsigned mn = 0, ms = 0;
 #pragma unroll
-        for (int q = 0; q < kSlotsPerGroup; ++q) {
-          const int sl = group * kSlotsPerGroup + q;
-          mn = max(mn, mx[sl]);
-          ms = max(ms, mx[8 + sl]);
+        for (int q = 0; q < 4; ++q) {
+          mn = max(mn, mx[4 * group + q]);
+          ms = max(ms, mx[16 + 4 * group + q]);
         }
         bmax = pair_bound(sc.coef, sm, __uint_as_float(ms), nm, __uint_as_float(mn));
       }
@@ -500,32 +511,41 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
       }
       if (!eok) continue;
       tc_fence_after();
-      for (int c = group * kGroupCols; c < (group + 1) * kGroupCols; c += 32) {
-        uint32_t v[32];
-        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + b * (uint32_t)kTN + (uint32_t)c, v);
-        const int col0 = t * sc.tile_stride * kTN + c;
-        float cmin = inf;     // pass 0: this chunk's smallest D over other columns
-        unsigned hmask = 0;   // column test: this chunk's hit columns (bit i)
-        // passes 2 and 3: D - B of every column of the group is at least
-        // RD(D - bmax); when that exceeds the row's limit and the column's
-        // list bar in every lane, no test can pass for the column
-        const float lim = kPass == 3 ? seed : t_row;
-#pragma unroll 4
-        for (int i = 0; i < 32; ++i) {
+      const int ctile = t * sc.tile_stride * kTN;
+      // passes 2 and 3: D - B of every column of the group is at least
+      // RD(D - bmax); when that exceeds the row's limit and the column's list
+      // bar in every lane, no test can pass for the column
+      const float lim = kPass == 3 ? seed : t_row;
+      float cmin = inf;    // pass 0: the 32-column chunk's smallest D over other columns
+      unsigned hmask = 0;  // column test: the chunk's hit columns (bit i)
+      // 16 columns from c (a half of a 32-column chunk: bits (c & 16) + i)
+      auto half = [&](uint32_t(&v)[16], int c) {
+        const int col0 = ctile + c, sh = c & 16;
+        // fast phase: D of the 16 columns (kept in v) and, for passes 2 and
+        // 3, a warp-uniform mask of the columns where some lane may pass a
+        // test; 16 independent chains without branches
+        unsigned need = kPass == 1 ? 0xffffu : 0u;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const float dv = __fsub_rn(__fadd_rn(nm, cn[c + i]), __fmul_rn(2.0f, __uint_as_float(v[i])));
+          v[i] = __float_as_uint(dv);
+          if (kKeepD && live && col0 + i < n) D[(long)m * ldD + col0 + i] = dv;
+          if (kPass == 0 && live && col0 + i < n && col0 + i != row) cmin = fminf(cmin, dv);
+          if (kPass == 2 || kPass == 3) {
+            const float wj = kPass == 3 ? cn[2 * kTN + c + i] : -inf;
+            if (__any_sync(0xffffffffu, __fsub_rd(dv, bmax) <= fmaxf(lim, wj))) need |= 1u << i;
+          }
+        }
+        // slow phase: the flagged columns (all of them for the heap pass),
+        // in column order, with their exact bounds
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          if (!((need >> i) & 1u)) continue;
+          const float dv = __uint_as_float(v[i]);
           const float nj = cn[c + i];
           const int j = col0 + i;
-          const float dv = __fsub_rn(__fadd_rn(nm, nj), __fmul_rn(2.0f, __uint_as_float(v[i])));
-          if (kKeepD && live && j < n) D[(long)m * ldD + j] = dv;
           const bool other = live && j < n && j != row;
-          if (kPass == 0) {
-            if (other) cmin = fminf(cmin, dv);
-            continue;
-          }
           const float wj = (kPass == 1 || kPass == 3) ? cn[2 * kTN + c + i] : -inf;
-          if (kPass == 2 || kPass == 3) {
-            const float lbq = __fsub_rd(dv, bmax);
-            if (!__any_sync(0xffffffffu, lbq <= fmaxf(lim, wj))) continue;
-          }
           const float sj = cn[kTN + c + i];
           const float bnd = pair_bound(sc.coef, sm, sj, nm, nj);
           if (kPass == 1 && other) {
@@ -543,14 +563,19 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
             }
           }
           if (col_test) {
-            if (live && j < sc.n_exist && __fsub_rd(dv, bnd) <= wj) hmask |= 1u << i;
+            if (live && j < sc.n_exist && __fsub_rd(dv, bnd) <= wj) hmask |= 1u << (sh + i);
           } else if (kPass == 2 && other && __fsub_rd(dv, bnd) <= t_row) {
             cand_m[atomicAdd(&sc.row_cnt[m], 1)] = j;
           }
         }
+      };
+      // after both halves of the 32-column chunk at c
+      auto chunk_end = [&](int c) {
+        const int col0 = ctile + c;
         if (kPass == 0 && live)
           sc.mins[(size_t)m * sc.mins_ld + t * (kTN / 32) + c / 32] =
               cmin == inf ? inf : fmaxf(__fadd_ru(cmin, bmax), 0.0f);
+        cmin = inf;
         if (col_test) {
           // the chunk's (existing row j, batch row m) pairs: one pool
           // reservation per warp, lanes in order
@@ -579,7 +604,25 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
               ++q;
             }
           }
+          hmask = 0;
         }
+      };
+      // the group's columns 16 at a time, the next half's tensor-memory load
+      // in flight while this half is screened
+      constexpr int kHalves = kGroupCols / 16;
+      const uint32_t ta = tmem + ((uint32_t)(quarter * 32) << 16) + b * (uint32_t)kTN +
+                          (uint32_t)(group * kGroupCols);
+      uint32_t va[16], vb[16];
+      tmem_ld16(ta, va);
+#pragma unroll 1
+      for (int h = 0; h < kHalves; h += 2) {
+        tmem_ld_wait(va);
+        tmem_ld16(ta + (uint32_t)(h + 1) * 16, vb);
+        half(va, group * kGroupCols + h * 16);
+        tmem_ld_wait(vb);
+        if (h + 2 < kHalves) tmem_ld16(ta + (uint32_t)(h + 2) * 16, va);
+        half(vb, group * kGroupCols + (h + 1) * 16);
+        chunk_end(group * kGroupCols + h * 16);
       }
       tc_fence_before();
       mbar_arrive(&tmem_empty[b]);
@@ -590,7 +633,7 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
     }
     if (kPass == 3) {
       // every group's stores to the row's counter are done
-      asm volatile("bar.sync 1, %0;" ::"n"(kEpi) : "memory");
+      asm volatile("bar.sync 5, %0;" ::"n"(kEpi) : "memory");
       if (group == 0 && live) {
         const int pcnt = scnt[r];
         sc.pre_cnt[(size_t)m * gridDim.x + blockIdx.x] = min(pcnt, sc.pre_cap);
@@ -700,10 +743,12 @@ __global__ void __launch_bounds__(kFinalWarps * 32)
 
 // Warp per batch row, after pass 3: T = the 32nd smallest stored upper
 // bound (exact: every column whose upper bound is at most T was stored),
-// then the row's candidates, the stored columns with lower bound <= T.  Lane
-// l walks segments l, l + 32, ...; entry i of every lane's segment is
-// handled together (four entries loaded ahead).  Does nothing when a segment
-// overflowed (the heap passes then run instead).
+// then the row's candidates, the stored columns with lower bound <= T.  With
+// 16 or more segments per row, lane l walks segments l, l + 32, ... and
+// entry i of every lane's segment is handled together; with fewer (longer)
+// segments the warp walks each segment's entries 32 at a time.  Four entries
+// are loaded ahead either way.  Does nothing when a segment overflowed (the
+// heap passes then run instead).
 __global__ void __launch_bounds__(kFinalWarps * 32)
     k_pre_select(const unsigned long long *pre, const float *pre_ub, const int *pre_cnt, int gx,
                  int cap, const int *pre_over, int nrows, int n, float *row_t, int *cand,
@@ -716,18 +761,23 @@ __global__ void __launch_bounds__(kFinalWarps * 32)
   const int m = blockIdx.x * kFinalWarps + (threadIdx.x >> 5);
   if (m >= nrows) return;
   const float inf = __int_as_float(0x7f800000);
+  const bool wide = gx >= 16;
+  // (segment, first entry, entry step) of this lane's walk over segment c
+  // of step cs
+  const int cs = wide ? 32 : 1, es = wide ? 1 : 32, e0 = wide ? 0 : lane;
   float top = inf;
-  for (int c0 = 0; c0 < gx; c0 += 32) {
-    const int c = c0 + lane;
+  for (int c0 = 0; c0 < gx; c0 += cs) {
+    const int c = wide ? c0 + lane : c0;
     const size_t seg = (size_t)m * gx + c;
     const int len = c < gx ? pre_cnt[seg] : 0;
     const float *u = pre_ub + seg * (size_t)cap;
     int maxlen = len;
-    for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
-    for (int i0 = 0; i0 < maxlen; i0 += 4) {
+    if (wide)
+      for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
+    for (int i0 = e0; i0 - e0 < maxlen; i0 += 4 * es) {
       float v[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) v[q] = i0 + q < len ? u[i0 + q] : inf;
+      for (int q = 0; q < 4; ++q) v[q] = i0 + q * es < len ? u[i0 + q * es] : inf;
 #pragma unroll
       for (int q = 0; q < 4; ++q) top32_merge(top, v[q], lane);
     }
@@ -736,20 +786,21 @@ __global__ void __launch_bounds__(kFinalWarps * 32)
   const float T = n - 1 < kListTop ? inf : __shfl_sync(0xffffffffu, top, 31);
   int *out = cand + (long)m * cand_ld;
   int cnt = 0;
-  for (int c0 = 0; c0 < gx; c0 += 32) {
-    const int c = c0 + lane;
+  for (int c0 = 0; c0 < gx; c0 += cs) {
+    const int c = wide ? c0 + lane : c0;
     const size_t seg = (size_t)m * gx + c;
     const int len = c < gx ? pre_cnt[seg] : 0;
     const unsigned long long *e = pre + seg * (size_t)cap;
     int maxlen = len;
-    for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
-    for (int i0 = 0; i0 < maxlen; i0 += 4) {
+    if (wide)
+      for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
+    for (int i0 = e0; i0 - e0 < maxlen; i0 += 4 * es) {
       unsigned long long v[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) v[q] = i0 + q < len ? e[i0 + q] : 0ull;
+      for (int q = 0; q < 4; ++q) v[q] = i0 + q * es < len ? e[i0 + q * es] : 0ull;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const bool keep = i0 + q < len && __uint_as_float((unsigned)(v[q] >> 32)) <= T;
+        const bool keep = i0 + q * es < len && __uint_as_float((unsigned)(v[q] >> 32)) <= T;
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
         if (keep) out[cnt + __popc(bal & ((1u << lane) - 1u))] = (int)(unsigned)v[q];
         cnt += __popc(bal);
@@ -1107,7 +1158,10 @@ void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int ro
   cudaMemsetAsync(x.row_cnt, 0, (size_t)nrows * sizeof(int), s);
   cudaMemsetAsync(x.counter, 0, sizeof(int), s);
   const int tiles = exact_seed_tiles(n_tiles);
-  if (n_tiles > 2 * kSeedTiles && x.pre && x.pre_cap > 0 && gx <= x.pre_gx &&
+  // entries per stored segment: the row's whole allocation shared by its
+  // tile's CTAs (fewer CTAs per row tile, longer segments)
+  const int cap = x.pre_fixed || gx > x.pre_gx ? x.pre_cap : (int)((long)x.pre_gx * x.pre_cap / gx);
+  if (n_tiles > 2 * kSeedTiles && x.pre && cap > 0 && gx <= x.pre_gx &&
       tiles * (kTN / 32) <= x.mins_ld) {
     // seed pass over a spread sample of tiles, then the store pass
     const int stride = n_tiles / tiles;
@@ -1119,12 +1173,12 @@ void launch_exact_dist(const DevState &st, const ExactMaps &maps, int dh, int ro
     cudaMemsetAsync(x.pre_over, 0, sizeof(int), s);
     if (kd)
       launch_tile<3, true>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, x.seed,
-                           x.pre_cap, 0, 0, nullptr, s);
+                           cap, 0, 0, nullptr, s);
     else
       launch_tile<3, false>(st, maps, dh, row0, blk0, nrows, n, x, ldD, gx, m_tiles, n_tiles, 1, x.seed,
-                            x.pre_cap, 0, 0, nullptr, s);
+                            cap, 0, 0, nullptr, s);
     k_pre_select<<<cdiv(nrows, kFinalWarps), kFinalWarps * 32, 0, s>>>(
-        x.pre, x.pre_ub, x.pre_cnt, gx, x.pre_cap, x.pre_over, nrows, n, x.row_t, x.cand, ldD, x.row_cnt,
+        x.pre, x.pre_ub, x.pre_cnt, gx, cap, x.pre_over, nrows, n, x.row_t, x.cand, ldD, x.row_cnt,
         st.stat);
     note_launch(2);
     // after an overflow only: the heap pass (seed-capped; its pairs were

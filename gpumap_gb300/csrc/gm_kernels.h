@@ -115,13 +115,15 @@ struct ExactScreen {
   float *seed = nullptr;      // rows thresholds from the seed pass
   float *mins = nullptr;       // rows x mins_ld chunk minima of the seed pass
   int mins_ld = 0;
-  // stored columns of the store pass: rows x pre_gx segments of pre_cap packed
-  // (lower bound, column) entries and their upper bounds, the segments'
-  // lengths, and an overflow flag
+  // stored columns of the store pass: per row pre_gx x pre_cap packed (lower
+  // bound, column) entries and their upper bounds, split into one segment
+  // per CTA of the row's tile (pre_gx x pre_cap / CTAs entries each, or
+  // pre_cap when pre_fixed), the segments' lengths, and an overflow flag
   unsigned long long *pre = nullptr;
   float *pre_ub = nullptr;
   int *pre_cnt = nullptr;
   int pre_cap = 0, pre_gx = 0;
+  bool pre_fixed = false;
   int *pre_over = nullptr;
   int *pool_j = nullptr, *pool_m = nullptr;    // column pairs as found
   int *pool_j2 = nullptr, *pool_m2 = nullptr;  // grouped by existing row

@@ -46,10 +46,12 @@ int gm_debug_copy(const struct gm_session *s, int which, void *host, uint64_t by
  * runs as the tile leaves the tensor memory and the tile is not stored. */
 int gm_debug_keep_tiles(struct gm_session *s, int on);
 /* Precision 1: entries per segment of stored columns that the store pass
- * over the tiles may keep (clamped to the 64 allocated; 0 runs the heap and
- * candidate passes instead, as for blocks of up to 32 column tiles).  A
- * segment that would exceed it makes the heap and candidate passes run for
- * its block (gm_stats.exact_overflow_blocks). */
+ * over the tiles may keep, fixed whatever the grid width (clamped to 64;
+ * by default each of a row tile's CTAs gets an equal share of the row's
+ * 64 x min(SMs, column tiles) entries; 0 runs the heap and candidate passes
+ * instead, as for blocks of up to 32 column tiles).  A segment that would
+ * exceed it makes the heap and candidate passes run for its block
+ * (gm_stats.exact_overflow_blocks). */
 int gm_debug_pre_capacity(struct gm_session *s, int cap);
 /* Host and device scalars, out[0..n):
  *  0 n_inserted, 1 insertion-queue head, 2 new-row embedding-queue head,

@@ -305,9 +305,10 @@ def test_exact_mode_seeded_screen_bitexact(native, oracle_mod, cap):
         same_state(s, o, tag=f"rows {c0}")
     same_state(s, o, embed=True, tag="final")
     over = s.stats().exact_overflow_blocks
-    # seeded blocks: the cycles at 9,000 rows and after (7 of them)
+    # seeded blocks: at least one in each cycle at 9,000 rows and after (7
+    # cycles; a 3,000-row batch may span several row blocks)
     if cap == 1:
-        assert over == 7, over
+        assert over >= 7, over
     else:
         assert over == 0, over
 

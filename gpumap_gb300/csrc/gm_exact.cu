@@ -158,6 +158,17 @@ GM_D void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
         "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
 }
+// One column of this thread's lane, waited for.
+GM_D uint32_t tmem_ld1(uint32_t taddr) {
+  uint32_t r;
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r)
+      : "r"(taddr)
+      : "memory");
+  return r;
+}
 GM_D void tmem_ld_wait(uint32_t (&r)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;"
                : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
@@ -518,17 +529,47 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
       const float lim = kPass == 3 ? seed : t_row;
       float cmin = inf;    // pass 0: the 32-column chunk's smallest D over other columns
       unsigned hmask = 0;  // column test: the chunk's hit columns (bit i)
-      // 16 columns from c (a half of a 32-column chunk: bits (c & 16) + i)
-      auto half = [&](uint32_t(&v)[16], int c) {
-        const int col0 = ctile + c, sh = c & 16;
-        // fast phase: D of the 16 columns (kept in v) and, for passes 2 and
-        // 3, a warp-uniform mask of the columns where some lane may pass a
-        // test; 16 independent chains without branches
-        unsigned need = kPass == 1 ? 0xffffu : 0u;
+      // the exact tests of column c + i of the tile (chunk bit (c & 16) + i),
+      // whose D is dv
+      auto slow = [&](int i, float dv, int c) {
+        const float nj = cn[c + i];
+        const int j = ctile + c + i;
+        const bool other = live && j < n && j != row;
+        const float wj = (kPass == 1 || kPass == 3) ? cn[2 * kTN + c + i] : -inf;
+        const float sj = cn[kTN + c + i];
+        const float bnd = pair_bound(sc.coef, sm, sj, nm, nj);
+        if (kPass == 1 && other) {
+          const float ub = fmaxf(__fadd_ru(dv, bnd), 0.0f);
+          if (ub < t_loc && ub <= seed) t_loc = heap_push(heap, hcnt, ub);
+        }
+        if (kPass == 3 && other) {
+          const float lb = __fsub_rd(dv, bnd);
+          if (lb <= seed) {
+            const int q = atomicAdd(&scnt[r], 1);
+            if (q < sc.pre_cap) {
+              sc.pre[seg + q] = ((unsigned long long)__float_as_uint(lb) << 32) | (unsigned)j;
+              sc.pre_ub[seg + q] = fmaxf(__fadd_ru(dv, bnd), 0.0f);
+            }
+          }
+        }
+        if (col_test) {
+          if (live && j < sc.n_exist && __fsub_rd(dv, bnd) <= wj) hmask |= 1u << ((c & 16) + i);
+        } else if (kPass == 2 && other && __fsub_rd(dv, bnd) <= t_row) {
+          cand_m[atomicAdd(&sc.row_cnt[m], 1)] = j;
+        }
+      };
+      // 16 columns from c (a half of a 32-column chunk), their accumulators
+      // in v and at tensor-memory address tah
+      auto half = [&](uint32_t(&v)[16], int c, uint32_t tah) {
+        const int col0 = ctile + c;
+        // fast phase: D of the 16 columns and, for passes 2 and 3, a
+        // warp-uniform mask of the columns where some lane may pass a test;
+        // 16 independent chains without branches
+        unsigned need = 0u;
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           const float dv = __fsub_rn(__fadd_rn(nm, cn[c + i]), __fmul_rn(2.0f, __uint_as_float(v[i])));
-          v[i] = __float_as_uint(dv);
+          if (kPass == 1) v[i] = __float_as_uint(dv);
           if (kKeepD && live && col0 + i < n) D[(long)m * ldD + col0 + i] = dv;
           if (kPass == 0 && live && col0 + i < n && col0 + i != row) cmin = fminf(cmin, dv);
           if (kPass == 2 || kPass == 3) {
@@ -536,36 +577,19 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
             if (__any_sync(0xffffffffu, __fsub_rd(dv, bmax) <= fmaxf(lim, wj))) need |= 1u << i;
           }
         }
-        // slow phase: the flagged columns (all of them for the heap pass),
-        // in column order, with their exact bounds
+        // slow phase, in column order: every column for the heap pass; for
+        // passes 2 and 3 only the flagged ones, each accumulator read again
+        // from tensor memory (D recomputed by the same operations), so that
+        // nothing of the fast phase stays live across it
+        if constexpr (kPass == 1) {
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          if (!((need >> i) & 1u)) continue;
-          const float dv = __uint_as_float(v[i]);
-          const float nj = cn[c + i];
-          const int j = col0 + i;
-          const bool other = live && j < n && j != row;
-          const float wj = (kPass == 1 || kPass == 3) ? cn[2 * kTN + c + i] : -inf;
-          const float sj = cn[kTN + c + i];
-          const float bnd = pair_bound(sc.coef, sm, sj, nm, nj);
-          if (kPass == 1 && other) {
-            const float ub = fmaxf(__fadd_ru(dv, bnd), 0.0f);
-            if (ub < t_loc && ub <= seed) t_loc = heap_push(heap, hcnt, ub);
-          }
-          if (kPass == 3 && other) {
-            const float lb = __fsub_rd(dv, bnd);
-            if (lb <= seed) {
-              const int q = atomicAdd(&scnt[r], 1);
-              if (q < sc.pre_cap) {
-                sc.pre[seg + q] = ((unsigned long long)__float_as_uint(lb) << 32) | (unsigned)j;
-                sc.pre_ub[seg + q] = fmaxf(__fadd_ru(dv, bnd), 0.0f);
-              }
-            }
-          }
-          if (col_test) {
-            if (live && j < sc.n_exist && __fsub_rd(dv, bnd) <= wj) hmask |= 1u << (sh + i);
-          } else if (kPass == 2 && other && __fsub_rd(dv, bnd) <= t_row) {
-            cand_m[atomicAdd(&sc.row_cnt[m], 1)] = j;
+          for (int i = 0; i < 16; ++i) slow(i, __uint_as_float(v[i]), c);
+        } else if constexpr (kPass == 2 || kPass == 3) {
+          while (need) {  // warp-uniform
+            const int i = __ffs(need) - 1;
+            need &= need - 1;
+            const float acc = __uint_as_float(tmem_ld1(tah + (uint32_t)i));
+            slow(i, __fsub_rn(__fadd_rn(nm, cn[c + i]), __fmul_rn(2.0f, acc)), c);
           }
         }
       };
@@ -618,10 +642,10 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
       for (int h = 0; h < kHalves; h += 2) {
         tmem_ld_wait(va);
         tmem_ld16(ta + (uint32_t)(h + 1) * 16, vb);
-        half(va, group * kGroupCols + h * 16);
+        half(va, group * kGroupCols + h * 16, ta + (uint32_t)h * 16);
         tmem_ld_wait(vb);
         if (h + 2 < kHalves) tmem_ld16(ta + (uint32_t)(h + 2) * 16, va);
-        half(vb, group * kGroupCols + (h + 1) * 16);
+        half(vb, group * kGroupCols + (h + 1) * 16, ta + (uint32_t)(h + 1) * 16);
         chunk_end(group * kGroupCols + h * 16);
       }
       tc_fence_before();

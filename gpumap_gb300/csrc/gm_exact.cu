@@ -767,12 +767,11 @@ __global__ void __launch_bounds__(kFinalWarps * 32)
 
 // Warp per batch row, after pass 3: T = the 32nd smallest stored upper
 // bound (exact: every column whose upper bound is at most T was stored),
-// then the row's candidates, the stored columns with lower bound <= T.  With
-// 16 or more segments per row, lane l walks segments l, l + 32, ... and
-// entry i of every lane's segment is handled together; with fewer (longer)
-// segments the warp walks each segment's entries 32 at a time.  Four entries
-// are loaded ahead either way.  Does nothing when a segment overflowed (the
-// heap passes then run instead).
+// then the row's candidates, the stored columns with lower bound <= T.  Lane
+// l walks segments l, l + 32, ... (a row tile has at least 19 CTAs on 152
+// SMs with blocks of up to 1,024 rows); entry i of every lane's segment is
+// handled together, four entries loaded ahead.  Does nothing when a segment
+// overflowed (the heap passes then run instead).
 __global__ void __launch_bounds__(kFinalWarps * 32)
     k_pre_select(const unsigned long long *pre, const float *pre_ub, const int *pre_cnt, int gx,
                  int cap, const int *pre_over, int nrows, int n, float *row_t, int *cand,
@@ -785,23 +784,18 @@ __global__ void __launch_bounds__(kFinalWarps * 32)
   const int m = blockIdx.x * kFinalWarps + (threadIdx.x >> 5);
   if (m >= nrows) return;
   const float inf = __int_as_float(0x7f800000);
-  const bool wide = gx >= 16;
-  // (segment, first entry, entry step) of this lane's walk over segment c
-  // of step cs
-  const int cs = wide ? 32 : 1, es = wide ? 1 : 32, e0 = wide ? 0 : lane;
   float top = inf;
-  for (int c0 = 0; c0 < gx; c0 += cs) {
-    const int c = wide ? c0 + lane : c0;
+  for (int c0 = 0; c0 < gx; c0 += 32) {
+    const int c = c0 + lane;
     const size_t seg = (size_t)m * gx + c;
     const int len = c < gx ? pre_cnt[seg] : 0;
     const float *u = pre_ub + seg * (size_t)cap;
     int maxlen = len;
-    if (wide)
-      for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
-    for (int i0 = e0; i0 - e0 < maxlen; i0 += 4 * es) {
+    for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
+    for (int i0 = 0; i0 < maxlen; i0 += 4) {
       float v[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) v[q] = i0 + q * es < len ? u[i0 + q * es] : inf;
+      for (int q = 0; q < 4; ++q) v[q] = i0 + q < len ? u[i0 + q] : inf;
 #pragma unroll
       for (int q = 0; q < 4; ++q) top32_merge(top, v[q], lane);
     }
@@ -810,21 +804,20 @@ __global__ void __launch_bounds__(kFinalWarps * 32)
   const float T = n - 1 < kListTop ? inf : __shfl_sync(0xffffffffu, top, 31);
   int *out = cand + (long)m * cand_ld;
   int cnt = 0;
-  for (int c0 = 0; c0 < gx; c0 += cs) {
-    const int c = wide ? c0 + lane : c0;
+  for (int c0 = 0; c0 < gx; c0 += 32) {
+    const int c = c0 + lane;
     const size_t seg = (size_t)m * gx + c;
     const int len = c < gx ? pre_cnt[seg] : 0;
     const unsigned long long *e = pre + seg * (size_t)cap;
     int maxlen = len;
-    if (wide)
-      for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
-    for (int i0 = e0; i0 - e0 < maxlen; i0 += 4 * es) {
+    for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(0xffffffffu, maxlen, o));
+    for (int i0 = 0; i0 < maxlen; i0 += 4) {
       unsigned long long v[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) v[q] = i0 + q * es < len ? e[i0 + q * es] : 0ull;
+      for (int q = 0; q < 4; ++q) v[q] = i0 + q < len ? e[i0 + q] : 0ull;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const bool keep = i0 + q * es < len && __uint_as_float((unsigned)(v[q] >> 32)) <= T;
+        const bool keep = i0 + q < len && __uint_as_float((unsigned)(v[q] >> 32)) <= T;
         const unsigned bal = __ballot_sync(0xffffffffu, keep);
         if (keep) out[cnt + __popc(bal & ((1u << lane) - 1u))] = (int)(unsigned)v[q];
         cnt += __popc(bal);

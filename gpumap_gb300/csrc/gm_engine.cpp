@@ -902,9 +902,21 @@ uint32_t Session::embed(uint32_t n_ops) {
   const int nu = ni - nb;
   const uint32_t *heur_idx = st_.pub_idx;
   const float *heur_dist = st_.pub_dist;
+  // the rows the reposition step moves (those not in the batch) and the
+  // SGD's row count depend only on the batch: queued before the phase
+  // waits for the previous one (after the schedule, whose compaction
+  // shares the flag scratch)
+  auto select_unsel = [&] {
+    launch_set_int(es_.iscal + kIscalN, ni, s);
+    if (nu <= 0) return;
+    ck(cudaMemsetAsync(es_.flag, 0, (size_t)ni * sizeof(int), s), "flags");
+    launch_mark_rows(es_.batch, nb, es_.flag, s);
+    compact_flags(es_.flag, ni, 0, es_.unsel, es_cnt_, es_.tmp, s);
+  };
   if (!p_.overlap) {
     launch_add_noise(st_.emb, ni, es_.batch, nb, 0.001f, noise_seed, es_, s);
     launch_schedule(ni, nb, k, p_.alpha, (int)p_.max_epoch, (int)p_.negative_sample_rate, es_, s);
+    select_unsel();
   } else {
     // the fuzzy set and schedule read only the published table: they run
     // beside the previous phase's SGD.  The reposition step reads the table
@@ -912,6 +924,7 @@ uint32_t Session::embed(uint32_t n_ops) {
     // runs).  Noise, the new rows' embedding and the SGD read the embedding
     // and wait for the previous phase.
     launch_schedule(ni, nb, k, p_.alpha, (int)p_.max_epoch, (int)p_.negative_sample_rate, es_, s);
+    select_unsel();
     if (nu > 0) {
       const size_t w = (size_t)ni * (size_t)(k + 1);
       ck(cudaMemcpyAsync(es_.pub_idx_snap, st_.pub_idx, w * sizeof(uint32_t), cudaMemcpyDeviceToDevice,
@@ -932,16 +945,10 @@ uint32_t Session::embed(uint32_t n_ops) {
     }
     launch_add_noise(st_.emb, ni, es_.batch, nb, 0.001f, noise_seed, es_, s);
   }
-  launch_set_int(es_.iscal + kIscalN, ni, s);
   timed_begin(2, s);
   run_sgd(s);
   timed_end(2, s);
-  if (nu > 0) {
-    ck(cudaMemsetAsync(es_.flag, 0, (size_t)ni * sizeof(int), s), "flags");
-    launch_mark_rows(es_.batch, nb, es_.flag, s);
-    compact_flags(es_.flag, ni, 0, es_.unsel, es_cnt_, es_.tmp, s);
-    launch_heuristic(heur_idx, heur_dist, ni, k, euclid, es_.unsel, nu, st_.emb, es_, s);
-  }
+  if (nu > 0) launch_heuristic(heur_idx, heur_dist, ni, k, euclid, es_.unsel, nu, st_.emb, es_, s);
   if (p_.overlap) {
     ck(cudaEventRecord(ev_emb_, s), "record embedding");
     emb_pending_ = true;

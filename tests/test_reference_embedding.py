@@ -6,9 +6,12 @@ the reference's compute_fuzzy_graph and run_optimize_layout run through
 oracle/refbuild/ref_embed_driver.cu (built from its unmodified sources), this
 build's gm_op_fuzzy_schedule and gm_op_sgd through the C ABI.  Both SGDs are
 Hogwild-parallel and draw their negative samples from different generators,
-so the embeddings are compared by their quality: trustworthiness and k-NN
-preservation within 0.01 of the reference's, the tolerance the engine is held
-to.  Skipped when the reference build is absent.
+so the embeddings are compared by their quality: the means over three runs
+of each of trustworthiness and k-NN preservation within 0.01 of the
+reference's, the tolerance the engine is held to.  (One run's k-NN
+preservation varies by about +-0.005 from run to run, in both builds; the
+means of five runs differed by 0.001-0.004 on these cases.)  Skipped when
+the reference build is absent.
 """
 import ctypes as C
 import subprocess
@@ -97,16 +100,19 @@ def test_embedding_quality_matches_reference(native, tmp_path, metric, n, d, k, 
     euclid = int(metric == "euclidean")
     pidx, pdst = _table(X, k, metric)
     emb0 = np.random.default_rng(seed).uniform(-10.0, 10.0, size=(n, 2)).astype(np.float32)
-    e_ref = _reference(tmp_path, pidx, pdst, emb0, k, euclid, 200, 5)
-    e_our = _ours(native, pidx, pdst, emb0, k, euclid, 200, 5)
-    assert np.all(np.isfinite(e_ref)) and np.all(np.isfinite(e_our))
     sample = np.arange(0, n, 2)
     q = 15
     # quality in the metric's own geometry (cosine: unit rows)
     Xq = X / np.linalg.norm(X, axis=1, keepdims=True) if metric == "cosine" else X
-    t_ref, t_our = trustworthiness(Xq, e_ref, q, sample=sample), trustworthiness(Xq, e_our, q, sample=sample)
-    p_ref = _knn_preservation(Xq, e_ref, q, sample, "euclidean")
-    p_our = _knn_preservation(Xq, e_our, q, sample, "euclidean")
+
+    def quality(e):
+        assert np.all(np.isfinite(e))
+        return trustworthiness(Xq, e, q, sample=sample), _knn_preservation(Xq, e, q, sample, "euclidean")
+
+    reps = 3
+    ref = np.mean([quality(_reference(tmp_path, pidx, pdst, emb0, k, euclid, 200, 5)) for _ in range(reps)], axis=0)
+    our = np.mean([quality(_ours(native, pidx, pdst, emb0, k, euclid, 200, 5)) for _ in range(reps)], axis=0)
+    (t_ref, p_ref), (t_our, p_our) = ref, our
     assert abs(t_our - t_ref) <= 0.01, (t_our, t_ref)
     assert abs(p_our - p_ref) <= 0.01, (p_our, p_ref)
     assert t_ref > 0.8, t_ref  # the reference itself embedded the clusters

@@ -238,10 +238,15 @@ __global__ void __launch_bounds__(kLJThreads, 3) k_local_join(
     if (nN == 0) continue;
     for (int c = t; c < nC; c += kLJThreads) S.nrm[c] = norms[S.cid[c]];
 
-    // ---- FP32 distance tile: rows N (4 per thread), cols N++O (8 per thread)
-    const int ty = t >> 4, tx = t & 15;
-    const int r0 = ty * 4, c0 = tx * 8;
-    const bool active = (r0 < nN) && (c0 < nC);
+    // ---- FP32 distance tile over the node's real extent (rows N, columns
+    // N ++ O): one 4 x 4 micro-tile per thread when the tile has at most
+    // kLJThreads of them (every node at k <= 16: about 30 x 90), else 4 x 8
+    // (at most 16 x 16); the threads past the last micro-tile only stage
+    const bool narrow = ((nN + 3) >> 2) * ((nC + 3) >> 2) <= kLJThreads;
+    const int mw = narrow ? 4 : 8;
+    const int mtc = (nC + mw - 1) / mw;
+    const bool active = t < ((nN + 3) >> 2) * mtc;
+    const int r0 = active ? (t / mtc) * 4 : 0, c0 = active ? (t % mtc) * mw : 0;
     float acc[4][8];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -294,13 +299,20 @@ __global__ void __launch_bounds__(kLJThreads, 3) k_local_join(
         for (int kk = 0; kk < kend; ++kk) {
           const float4 a = *reinterpret_cast<const float4 *>(&S.As[kk][r0]);
           const float4 b0 = *reinterpret_cast<const float4 *>(&S.Bs[kk][c0]);
-          const float4 b1 = *reinterpret_cast<const float4 *>(&S.Bs[kk][c0 + 4]);
           const float av[4] = {a.x, a.y, a.z, a.w};
-          const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+          const float bv[4] = {b0.x, b0.y, b0.z, b0.w};
 #pragma unroll
           for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int j = 0; j < 8; ++j) acc[i][j] = __fmaf_rn(av[i], bv[j], acc[i][j]);
+            for (int j = 0; j < 4; ++j) acc[i][j] = __fmaf_rn(av[i], bv[j], acc[i][j]);
+          if (!narrow) {
+            const float4 b1 = *reinterpret_cast<const float4 *>(&S.Bs[kk][c0 + 4]);
+            const float bw[4] = {b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+              for (int j = 0; j < 4; ++j) acc[i][4 + j] = __fmaf_rn(av[i], bw[j], acc[i][4 + j]);
+          }
         }
       }
       __syncthreads();
@@ -311,7 +323,7 @@ __global__ void __launch_bounds__(kLJThreads, 3) k_local_join(
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           const int r = r0 + i, c = c0 + j;
-          if (r < nN && c < nC) S.D[r][c] = canon_dist(S.nrm[r], S.nrm[c], acc[i][j]);
+          if (j < mw && r < nN && c < nC) S.D[r][c] = canon_dist(S.nrm[r], S.nrm[c], acc[i][j]);
         }
     }
     __syncthreads();

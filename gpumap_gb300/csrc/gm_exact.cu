@@ -57,7 +57,7 @@ __host__ __device__ constexpr int exact_threads(int pass) { return 64 + 128 * ex
 constexpr int kTmemCols = 512;                 // two 128 x 256 FP32 accumulators
 constexpr uint32_t kWaitLimit = 1u << 24;      // bounded mbarrier waits
 // epilogue column buffer: the 256 columns' squared norms, bound factors and
-// list bars of a tile, double buffered (two tiles), then per buffer eight
+// list bars of a tile, double buffered (two tiles), then per buffer sixteen
 // per-warp maxima of the norms and bound factors (float bits: both >= 0)
 constexpr size_t kEpiBytes = (size_t)2 * 3 * kTN * sizeof(float) + (size_t)2 * 2 * 16 * sizeof(float);
 constexpr int kListTop = 32;                   // list width the screen keeps exact
@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(exact_threads(kPass), 1)
     __syncwarp();
   } else {
     // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (tile rows), one row
-    // per thread, 32 columns per tcgen05.ld; warp group g = (w - 2) / 4
+    // per thread, 16 columns per tcgen05.ld; warp group g = (w - 2) / 4
     // takes columns [g * kGroupCols, +kGroupCols) of each tile.  Each group
     // loads its columns' data (squared norms, bound factors, list bars) one
     // tile ahead into a double-buffered shared array that its lanes read by

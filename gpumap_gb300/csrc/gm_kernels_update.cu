@@ -164,12 +164,20 @@ constexpr int kLJKC = 32;
 constexpr int kLJR = kJoinMax;      // 64 tile rows (N)
 constexpr int kLJC = 2 * kJoinMax;  // 128 tile cols (N ++ O)
 
+// One feature chunk of the node's rows: N (A) and N ++ O (B), feature-major.
+struct LJStage {
+  float As[kLJKC][kLJR + 4];
+  float Bs[kLJKC][kLJC + 4];
+};
 struct LJSmem {
   int cid[kLJC];
   float nrm[kLJC];
-  float As[kLJKC][kLJR + 4];
-  float Bs[kLJKC][kLJC + 4];
-  float D[kLJR][kLJC + 1];
+  // two chunk stages (chunk i in stage i & 1: one barrier per chunk), and
+  // over them, once the products are done, the node's distance tile
+  union {
+    LJStage st[2];
+    float D[kLJR][kLJC + 1];
+  } u;
   Key lst[kLJWarps][kListW];
   Key cb[kLJWarps][kLJC];
   int nN, nC;
@@ -276,29 +284,34 @@ __global__ void __launch_bounds__(kLJThreads, 3) k_local_join(
           pb[p] = __ldg(reinterpret_cast<const float4 *>(X + (size_t)S.cid[r] * ld + col));
       }
     };
+    // chunk i is stored in stage i & 1, whose last readers (the products of
+    // chunk i - 2) every thread has finished before the barrier of chunk
+    // i - 1, so one barrier per chunk orders both uses
     fetch(0);
-    for (int k0 = 0; k0 < d; k0 += kLJKC) {
+    int sb = 0;
+    for (int k0 = 0; k0 < d; k0 += kLJKC, sb ^= 1) {
+      LJStage &G = S.u.st[sb];
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
         const int f = t + p * kLJThreads;
         const int r = f >> 3, q = f & 7;
-        S.As[4 * q][r] = pa[p].x; S.As[4 * q + 1][r] = pa[p].y;
-        S.As[4 * q + 2][r] = pa[p].z; S.As[4 * q + 3][r] = pa[p].w;
+        G.As[4 * q][r] = pa[p].x; G.As[4 * q + 1][r] = pa[p].y;
+        G.As[4 * q + 2][r] = pa[p].z; G.As[4 * q + 3][r] = pa[p].w;
       }
 #pragma unroll
       for (int p = 0; p < 4; ++p) {
         const int f = t + p * kLJThreads;
         const int r = f >> 3, q = f & 7;
-        S.Bs[4 * q][r] = pb[p].x; S.Bs[4 * q + 1][r] = pb[p].y;
-        S.Bs[4 * q + 2][r] = pb[p].z; S.Bs[4 * q + 3][r] = pb[p].w;
+        G.Bs[4 * q][r] = pb[p].x; G.Bs[4 * q + 1][r] = pb[p].y;
+        G.Bs[4 * q + 2][r] = pb[p].z; G.Bs[4 * q + 3][r] = pb[p].w;
       }
       __syncthreads();
       if (k0 + kLJKC < d) fetch(k0 + kLJKC);
       if (active) {
         const int kend = min(kLJKC, d - k0);
         for (int kk = 0; kk < kend; ++kk) {
-          const float4 a = *reinterpret_cast<const float4 *>(&S.As[kk][r0]);
-          const float4 b0 = *reinterpret_cast<const float4 *>(&S.Bs[kk][c0]);
+          const float4 a = *reinterpret_cast<const float4 *>(&G.As[kk][r0]);
+          const float4 b0 = *reinterpret_cast<const float4 *>(&G.Bs[kk][c0]);
           const float av[4] = {a.x, a.y, a.z, a.w};
           const float bv[4] = {b0.x, b0.y, b0.z, b0.w};
 #pragma unroll
@@ -306,7 +319,7 @@ __global__ void __launch_bounds__(kLJThreads, 3) k_local_join(
 #pragma unroll
             for (int j = 0; j < 4; ++j) acc[i][j] = __fmaf_rn(av[i], bv[j], acc[i][j]);
           if (!narrow) {
-            const float4 b1 = *reinterpret_cast<const float4 *>(&S.Bs[kk][c0 + 4]);
+            const float4 b1 = *reinterpret_cast<const float4 *>(&G.Bs[kk][c0 + 4]);
             const float bw[4] = {b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
             for (int i = 0; i < 4; ++i)
@@ -315,15 +328,15 @@ __global__ void __launch_bounds__(kLJThreads, 3) k_local_join(
           }
         }
       }
-      __syncthreads();
     }
+    __syncthreads();  // every product is done before the tile overwrites the stages
     if (active) {
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           const int r = r0 + i, c = c0 + j;
-          if (j < mw && r < nN && c < nC) S.D[r][c] = canon_dist(S.nrm[r], S.nrm[c], acc[i][j]);
+          if (j < mw && r < nN && c < nC) S.u.D[r][c] = canon_dist(S.nrm[r], S.nrm[c], acc[i][j]);
         }
     }
     __syncthreads();
@@ -345,7 +358,7 @@ __global__ void __launch_bounds__(kLJThreads, 3) k_local_join(
         Key ck = 0;
         if (c < ncand && c != tt) {
           const int cidv = S.cid[c];
-          const float dv = (tt < nN) ? S.D[tt][c] : S.D[c][tt];
+          const float dv = (tt < nN) ? S.u.D[tt][c] : S.u.D[c][tt];
           ck = make_key(dv, cidv);
           if (cidv != idt && ck < worst) {
             pass = true;

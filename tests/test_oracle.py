@@ -130,6 +130,27 @@ def test_progressive_cycles_and_queues(oracle_mod):
     assert recall_at_k(o.neighbor_indices(2000), ei) > 0.95
 
 
+@pytest.mark.parametrize("metric", [0, 1])
+def test_exact_insertion_matches_fp64_brute_force(oracle_mod, metric):
+    # precision 1 (the oracle of the tensor-core exact insertion): after
+    # progressive cycles every published list is the exact k nearest among
+    # all rows, distances in the published convention (squared L2, or
+    # 2 (1 - cos)) and ascending; only FP32 ties may reorder against FP64
+    n, d, k = 900, 20, 15
+    X, _ = gaussian_mixture(n, d, seed=12)
+    o = oracle_mod.OracleSession(n, d, k=k, metric=metric, max_epoch=5, precision=1)
+    for c0 in range(0, n, 300):
+        o.append(X[c0 : c0 + 300])
+        r = o.run(300, 0, 0)
+        assert r["n_inserted_instances"] == c0 + 300
+    idx = o.neighbor_indices(n).astype(np.int64)
+    dst = o.neighbor_dists(n).astype(np.float64)
+    ei, ed = exact_knn(X, k, metric="cosine" if metric else "euclidean")
+    assert recall_at_k(idx, ei) > 0.999
+    assert np.all(np.diff(dst, axis=1) >= 0)
+    np.testing.assert_allclose(dst, ed, rtol=1e-4, atol=1e-5)
+
+
 def test_cosine_rows_normalised(oracle_mod):
     rng = np.random.default_rng(5)
     X = rng.normal(size=(300, 20)).astype(np.float32) * 3

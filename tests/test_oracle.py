@@ -130,13 +130,13 @@ def test_progressive_cycles_and_queues(oracle_mod):
     assert recall_at_k(o.neighbor_indices(2000), ei) > 0.95
 
 
-@pytest.mark.parametrize("metric", [0, 1])
-def test_exact_insertion_matches_fp64_brute_force(oracle_mod, metric):
+@pytest.mark.parametrize("metric,k", [(0, 15), (1, 15), (1, 30)])
+def test_exact_insertion_matches_fp64_brute_force(oracle_mod, metric, k):
     # precision 1 (the oracle of the tensor-core exact insertion): after
     # progressive cycles every published list is the exact k nearest among
     # all rows, distances in the published convention (squared L2, or
     # 2 (1 - cos)) and ascending; only FP32 ties may reorder against FP64
-    n, d, k = 900, 20, 15
+    n, d = 900, 20
     X, _ = gaussian_mixture(n, d, seed=12)
     o = oracle_mod.OracleSession(n, d, k=k, metric=metric, max_epoch=5, precision=1)
     for c0 in range(0, n, 300):
@@ -149,6 +149,26 @@ def test_exact_insertion_matches_fp64_brute_force(oracle_mod, metric):
     assert recall_at_k(idx, ei) > 0.999
     assert np.all(np.diff(dst, axis=1) >= 0)
     np.testing.assert_allclose(dst, ed, rtol=1e-4, atol=1e-5)
+
+
+def test_exact_insertion_orders_duplicates_by_id(oracle_mod):
+    # rows repeated exactly: a row's copies are at distance 0 and come first,
+    # ties broken by id as the packed (distance, id) keys order them
+    rng = np.random.default_rng(9)
+    base = rng.normal(size=(100, 8)).astype(np.float32)
+    X = np.concatenate([base, base, base])  # row r has copies r + 100, r + 200
+    n, k = len(X), 10
+    o = oracle_mod.OracleSession(n, 8, k=k, precision=1, max_epoch=5)
+    o.append(X)
+    o.run(n, 0, 0)
+    idx = o.neighbor_indices(n).astype(np.int64)
+    dst = o.neighbor_dists(n)
+    for r in (0, 57, 199, 250):
+        copies = sorted({r % 100, r % 100 + 100, r % 100 + 200} - {r})
+        assert idx[r, :2].tolist() == copies, (r, idx[r, :3])
+        assert np.all(dst[r, :2] == 0.0)
+        assert np.all(np.diff(dst[r]) >= 0)
+        assert len(set(idx[r].tolist())) == k and r not in idx[r]
 
 
 def test_cosine_rows_normalised(oracle_mod):
